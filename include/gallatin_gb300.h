@@ -1,0 +1,201 @@
+/*
+ * gallatin_gb300.h — C ABI of the GB300-native Gallatin-compatible device allocator.
+ *
+ * Every entry point takes plain pointers and sizes and returns an int status
+ * (GAL_OK == 0, otherwise one of the GAL_ERR_* codes below).  Device buffers are
+ * raw CUDA device pointers; `stream` is a cudaStream_t passed as void* (NULL =
+ * legacy default stream).  No C++ or torch types appear in these signatures.
+ *
+ * The reference (chillenzer/gallatin) is a header-only CUDA C++ library with no
+ * FFI of its own.  Each function below names the reference interface it stands
+ * in for (path:line inside the reference project).  The device-side malloc/free
+ * stay header-inline (include/gallatin_gb300/gal_device.cuh and the drop-in
+ * headers under include/gallatin/allocators/) because a device function cannot
+ * cross a C ABI.
+ */
+#ifndef GALLATIN_GB300_H
+#define GALLATIN_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define GAL_OK               0
+#define GAL_ERR_ARGS         1   /* invalid argument / size out of range            */
+#define GAL_ERR_CUDA         2   /* a CUDA runtime call failed                       */
+#define GAL_ERR_OOM          3   /* device memory for arena/metadata not available   */
+#define GAL_ERR_STATE        4   /* handle not initialised / already initialised     */
+#define GAL_ERR_DEVICE       5   /* the device error word is non-zero (see below)    */
+
+/* ---- device error word bits (gal_last_error) ----------------------------- */
+#define GAL_DEV_ERR_TIMEOUT        0x1u  /* a bounded spin-wait gave up             */
+#define GAL_DEV_ERR_BAD_FREE       0x2u  /* free of a pointer in a free segment      */
+#define GAL_DEV_ERR_NULL_QUEUE     0x4u  /* recycle ring slot empty on hand-out      */
+#define GAL_DEV_ERR_SEGMENT_SETUP  0x8u  /* segment tree id claim failed             */
+#define GAL_DEV_ERR_SLOT_SWAP      0x10u /* pinned slot swap-in found a block        */
+#define GAL_DEV_ERR_BLOCK_TREE     0x20u /* whole-block fill saw a foreign tree id   */
+#define GAL_DEV_ERR_BOOT           0x40u /* boot could not fill a pinned slot        */
+
+/* ---- sub-tree (size class) segment choice --------------------------------- */
+#define GAL_POLICY_REFERENCE 0u  /* Murmur-hashed start, as gallatin veb.cuh:946-977 */
+#define GAL_POLICY_LOWEST    1u  /* always the smallest segment id with free blocks */
+
+/* ---- limits --------------------------------------------------------------- */
+#define GAL_MAX_TREES        16
+#define GAL_MAX_VEB_LAYERS   8
+
+/* Runtime configuration.  The three geometry fields are the reference's
+ * template parameters Gallatin<bytes_per_segment, smallest, biggest>
+ * (gallatin.cuh:292); all three must be powers of two and
+ * bytes_per_segment >= max_size*4096 (gallatin.cuh:300). */
+typedef struct gal_config {
+  uint64_t bytes_per_segment;   /* default 16 MiB                                  */
+  uint64_t min_size;            /* default 16 B                                    */
+  uint64_t max_size;            /* default 4096 B                                  */
+  int32_t  smid_override;       /* -1: pinned slot from %smid; >=0: fixed value   */
+  uint32_t subtree_policy;      /* GAL_POLICY_*                                    */
+  uint32_t pinned_slots_first;  /* pinned slots of tree 0 (reference: 128)        */
+  uint32_t pinned_slots_min;    /* floor when halving per tree (reference: 4)     */
+  uint32_t zero_arena;          /* 1: memset the arena at init (reference does)   */
+  uint32_t spin_limit;          /* iteration cap for every device spin-wait       */
+} gal_config;
+
+/* Aggregate statistics (stands in for Gallatin::print_info, gallatin.cuh:1855). */
+typedef struct gal_stats {
+  uint64_t num_segments;
+  uint64_t free_segments;                 /* set bits of the segment tree        */
+  uint64_t largest_free_run;              /* longest run of free segments        */
+  uint32_t num_trees;
+  uint32_t error_word;
+  uint64_t tree_segments[GAL_MAX_TREES];  /* segments owned (table tree id)      */
+  uint64_t tree_listed[GAL_MAX_TREES];    /* set bits of each size-class tree    */
+  uint64_t tree_live_blocks[GAL_MAX_TREES];
+  uint64_t multi_segment_allocs;          /* live multi-segment allocations     */
+  uint64_t multi_segment_segments;        /* segments they cover                 */
+  uint64_t metadata_bytes;                /* device bytes of allocator metadata  */
+} gal_stats;
+
+/* Dimensions of the host-side state view (sizes of the arrays below). */
+typedef struct gal_state_dims {
+  uint64_t num_segments;        /* S                                              */
+  uint32_t num_trees;           /* T                                              */
+  uint32_t blocks_per_segment;  /* table stride: bytes_per_segment/(min*4096)     */
+  uint32_t veb_layers;          /* layers of every vEB tree (universe S)          */
+  uint32_t veb_words;           /* 64-bit words of one tree, all layers           */
+  uint32_t total_slots;         /* pinned slots summed over trees                 */
+  uint32_t slot_counts[GAL_MAX_TREES];
+} gal_state_dims;
+
+/* Host-side, layout-neutral copy of the whole allocator state, in the
+ * reference's value conventions so that states from the reference build, the
+ * CPU oracle and this library compare word for word:
+ *   - vEB words: per tree, layer 0 (top) first, each layer ceil(u/64) words;
+ *   - malloc_counters: (tree << 20) | count, as gallatin block.cuh:53,220;
+ *   - queues / slots: global block id, or -1 for an empty entry (nullptr).
+ * The caller owns every buffer; sizes follow gal_state_dims. */
+typedef struct gal_state_view {
+  uint64_t *seg_tree_words;             /* [veb_words]                     */
+  uint64_t *sub_tree_words;             /* [num_trees * veb_words]         */
+  uint16_t *tree_ids;                   /* [S], 0xFFFF = free              */
+  int32_t  *active_counts;              /* [S]                             */
+  uint32_t *queue_counters;             /* [S]                             */
+  uint32_t *queue_free_counters;        /* [S]                             */
+  uint32_t *final_queue_free_counters;  /* [S]                             */
+  uint32_t *malloc_counters;            /* [S * blocks_per_segment]        */
+  uint32_t *free_counters;              /* [S * blocks_per_segment]        */
+  int32_t  *queues;                     /* [S * blocks_per_segment]        */
+  int32_t  *slots;                      /* [total_slots]                   */
+  uint32_t  locks;
+  uint32_t  error_word;
+} gal_state_view;
+
+typedef struct gal_handle gal_handle;
+
+/* Fill *cfg with the reference defaults: <16 MiB, 16, 4096>, 128/4 pinned
+ * slots, reference sub-tree policy, hardware %smid, zeroed arena. */
+int gal_config_default(gal_config *cfg);
+
+/* Build an allocator over `num_bytes` of device memory on the current device.
+ * Replaces Gallatin<>::generate_on_device (gallatin.cuh:324-421).  The pinned
+ * slots are booted deterministically in the order of the reference's
+ * boot_shared_block_container_one_thread (gallatin.cuh:196-221). */
+int gal_create(uint64_t num_bytes, uint64_t seed, const gal_config *cfg, gal_handle **out);
+
+/* Same as gal_create without the boot (pinned slots empty); for state import. */
+int gal_create_unbooted(uint64_t num_bytes, uint64_t seed, const gal_config *cfg, gal_handle **out);
+
+/* Release arena and metadata.  Replaces Gallatin<>::free_on_device
+ * (gallatin.cuh:643-668).  Pointers handed out become invalid. */
+int gal_destroy(gal_handle *h);
+
+/* Device pointer to the allocator object (what a Gallatin<>* points to). */
+void *gal_device_state(gal_handle *h);
+/* Device pointer to the first byte of the arena (alloc_table::memory,
+ * memory_table.cuh:255). */
+void *gal_arena_base(gal_handle *h);
+/* Bytes covered by the arena (num_segments * bytes_per_segment). */
+uint64_t gal_arena_bytes(gal_handle *h);
+
+/* Replaces print_global_stats / Gallatin::print_info
+ * (global_allocator.cuh:86-97, gallatin.cuh:1855-1897). */
+int gal_get_stats(gal_handle *h, gal_stats *out);
+int gal_print_stats(gal_handle *h);
+
+/* Device error word (GAL_DEV_ERR_* bits); replaces the reference's `trap`
+ * on invariant breaks (gallatin.cuh:87). */
+int gal_last_error(gal_handle *h, uint32_t *out_bits);
+int gal_clear_error(gal_handle *h);
+
+/* State view export/import (no reference counterpart: test and drain-check
+ * support, SURVEY-style "snapshot"). */
+int gal_state_dims_get(gal_handle *h, gal_state_dims *out);
+int gal_export_state(gal_handle *h, const gal_state_view *view);
+int gal_import_state(gal_handle *h, const gal_state_view *view);
+
+/* Change the pinned-slot smid override after creation (-1 = hardware). */
+int gal_set_smid_override(gal_handle *h, int32_t smid);
+/* Change the sub-tree policy after creation (GAL_POLICY_*). */
+int gal_set_policy(gal_handle *h, uint32_t policy);
+
+/* ---- process-global instance (drop-in init/teardown) ---------------------- */
+/* Replaces init_global_allocator (global_allocator.cuh:48-56). */
+int gal_init(uint64_t num_bytes, uint64_t seed, const gal_config *cfg);
+/* Replaces free_global_allocator (global_allocator.cuh:59-70). */
+int gal_teardown(void);
+/* The global handle (NULL before gal_init). */
+gal_handle *gal_global(void);
+
+/* ---- device work launched by the library ---------------------------------- */
+
+/* Serial replay of an op trace by one device thread, the single-thread test of
+ * the reference (tests/src/gallatin_single_thread.cu:38-93) generalised.
+ * ops[i]: bit 63 clear → malloc(ops[i]); bit 63 set → free of the pointer
+ * returned by op (ops[i] & ~bit63).  out_offsets[i] = pointer - arena base for
+ * a malloc (UINT64_MAX for nullptr), UINT64_MAX for a free.  out_smid[0] =
+ * %smid the thread ran on.  All buffers are device pointers. */
+int gal_replay_trace(gal_handle *h, const uint64_t *ops, uint64_t nops,
+                     uint64_t *out_offsets, uint32_t *out_smid, void *stream);
+
+/* One device thread per request: out_ptrs[i] = malloc(sizes[i]) (per-thread
+ * global_malloc, global_allocator.cuh:72-76). */
+int gal_malloc_per_thread(gal_handle *h, const uint64_t *sizes, uint64_t n,
+                          void **out_ptrs, void *stream);
+/* One device thread per pointer: free(ptrs[i]) unless NULL
+ * (global_free, global_allocator.cuh:78-82). */
+int gal_free_per_thread(gal_handle *h, void *const *ptrs, uint64_t n, void *stream);
+
+/* Batched form: the same results contract as gal_malloc_per_thread, served by
+ * CTA-level aggregation (one claim per size class per CTA). */
+int gal_malloc_batched(gal_handle *h, const uint64_t *sizes, uint64_t n,
+                       void **out_ptrs, void *stream);
+int gal_free_batched(gal_handle *h, void *const *ptrs, uint64_t n, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GALLATIN_GB300_H */

@@ -1,0 +1,814 @@
+// gal_device.cuh — device side of the GB300-native Gallatin-compatible allocator.
+//
+// Header-inline because device malloc/free run inside the caller's kernels.
+// The host side (construction, teardown, stats, state export) is the C ABI in
+// include/gallatin_gb300.h; the drop-in C++ API is include/gallatin/allocators/.
+//
+// Algorithm: the reference allocator (chillenzer/gallatin,
+// include/gallatin/allocators/gallatin.cuh and friends), restated so a serial
+// trace returns the reference's offsets byte for byte.  Layout and
+// synchronisation are this library's own:
+//   * all metadata in one device region addressed from one state struct
+//     (no pointer chasing through per-structure objects);
+//   * blocks, queue entries and pinned slots are 32-bit block ids, not Block*;
+//   * the malloc word of a block is 64-bit: (tree << 32) | count, so stale
+//     claims can never carry a count into the tree field (the reference packs
+//     tree << 20 | count into 32 bits, block.cuh:53);
+//   * malloc and free counters live in separate arrays (different L2 lines);
+//   * every spin-wait is bounded by state::spin_limit and reports through the
+//     error word instead of trapping (the reference traps, gallatin.cuh:87);
+//   * a vEB remove re-checks the emptied child word after clearing its
+//     summary bit, closing the race that hides a non-empty word;
+//   * a failed contiguous-run search does not roll back bits it never took
+//     (the reference's exit rollback, veb.cuh:447);
+//   * a multi-segment free resets the segment's tree id before returning its
+//     bits, so a concurrent claim never meets a stale id (gallatin.cuh:1283-1302
+//     returns the bits first).
+#pragma once
+
+#include <stdint.h>
+
+#include "../gallatin_gb300.h"
+
+#ifndef GAL_DEVICE_INLINE
+#define GAL_DEVICE_INLINE __device__ __forceinline__
+#endif
+#define GAL_DEVICE_COLD __device__ __noinline__
+
+namespace gal {
+
+static constexpr uint32_t NOBLK = 0xFFFFFFFFu;
+static constexpr uint64_t FAIL = ~0ULL;
+static constexpr uint16_t FREE_TREE = 0xFFFF;
+static constexpr uint32_t SLICES_PER_BLOCK = 4096;
+
+// retry caps of the reference (gallatin.cuh:108-112, veb.cuh:59)
+static constexpr int SLICE_ATTEMPTS = 500 * 10;
+static constexpr int VEB_ATTEMPTS = 15;
+static constexpr int GATHER_RETRIES = 8;
+static constexpr int BLOCK_ATTEMPTS = 8;
+static constexpr int SEGMENT_ATTEMPTS = 8;
+static constexpr int SLOT_PROBE_LIMIT = 30;  // SHARED_BLOCK_COUNTER_CUTOFF
+
+struct veb_shape {
+  uint32_t layers;
+  uint32_t words;                        // words of one tree, all layers
+  uint32_t off[GAL_MAX_VEB_LAYERS];      // word offset of each layer (0 = top)
+  uint32_t nwords[GAL_MAX_VEB_LAYERS];
+  uint64_t items[GAL_MAX_VEB_LAYERS];    // universe of each layer
+};
+
+// Everything a kernel needs; lives in device memory (the object a
+// Gallatin<>* points to) and may also be passed by value as a kernel param.
+struct state {
+  char *memory;
+  uint64_t num_segments;
+  uint64_t seed;
+  uint32_t seg_shift;   // log2 bytes_per_segment
+  uint32_t min_shift;   // log2 min_size
+  uint32_t bps_shift;   // log2 table blocks per segment
+  uint32_t num_trees;
+  uint32_t policy;
+  int32_t smid_override;
+  uint32_t spin_limit;
+  uint32_t total_slots;
+  uint32_t slot_base[GAL_MAX_TREES];
+  uint32_t slot_count[GAL_MAX_TREES];
+  veb_shape veb;
+  uint64_t *seg_tree;            // [veb.words]
+  uint64_t *sub_trees;           // [num_trees * veb.words]
+  uint16_t *tree_ids;            // [S]
+  int32_t *active;               // [S] blocks left to hand out, minus one
+  uint32_t *qc;                  // [S] hand-out position
+  uint32_t *qfc;                 // [S] return position
+  uint32_t *fqfc;                // [S] finalised return position
+  unsigned long long *mwords;    // [S << bps_shift] (tree << 32) | count
+  uint32_t *fctr;                // [S << bps_shift] frees counted
+  uint32_t *queues;              // [S << bps_shift] recycle ring (block ids)
+  uint32_t *slots;               // [total_slots] pinned blocks
+  uint32_t *locks;               // tree locks (bit t) + bit num_trees for runs
+  uint32_t *error;               // GAL_DEV_ERR_* bits
+};
+
+// ------------------------------------------------------------------ helpers
+GAL_DEVICE_INLINE uint32_t lane_id() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%laneid;" : "=r"(r));
+  return r;
+}
+GAL_DEVICE_INLINE uint32_t lanemask_lt() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(r));
+  return r;
+}
+GAL_DEVICE_INLINE uint32_t sm_id() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%smid;" : "=r"(r));
+  return r;
+}
+GAL_DEVICE_INLINE uint64_t ld_rlx(const uint64_t *p) {
+  uint64_t v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+GAL_DEVICE_INLINE uint32_t ld_rlx(const uint32_t *p) {
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+GAL_DEVICE_INLINE int32_t ld_rlx(const int32_t *p) {
+  return (int32_t)ld_rlx((const uint32_t *)p);
+}
+GAL_DEVICE_INLINE uint16_t ld_rlx(const uint16_t *p) {
+  uint16_t v;
+  asm volatile("ld.relaxed.gpu.global.u16 %0, [%1];" : "=h"(v) : "l"(p) : "memory");
+  return v;
+}
+GAL_DEVICE_INLINE uint64_t amo_or(uint64_t *p, uint64_t v) {
+  return atomicOr((unsigned long long *)p, (unsigned long long)v);
+}
+GAL_DEVICE_INLINE uint64_t amo_and(uint64_t *p, uint64_t v) {
+  return atomicAnd((unsigned long long *)p, (unsigned long long)v);
+}
+GAL_DEVICE_INLINE uint16_t cas16(uint16_t *p, uint16_t cmp, uint16_t val) {
+  return (uint16_t)atomicCAS((unsigned short *)p, (unsigned short)cmp, (unsigned short)val);
+}
+GAL_DEVICE_INLINE void set_error(const state *s, uint32_t bits) { atomicOr(s->error, bits); }
+GAL_DEVICE_INLINE void backoff(uint32_t i) { __nanosleep(i < 8 ? 32u << i : 4096u); }
+
+// ceil(log2(x)) for x > 0, 0 for x == 0 (alloc_utils.cuh:382-398)
+GAL_DEVICE_INLINE int ceil_log2(uint64_t x) {
+  return 63 - __clzll((long long)x) + (__popcll(x) != 1);
+}
+
+// MurmurHash64A (Austin Appleby, public domain) of one 8-byte key
+GAL_DEVICE_INLINE uint64_t murmur64a_u64(uint64_t key, uint64_t seed) {
+  const uint64_t m = 0xc6a4a7935bd1e995ULL;
+  uint64_t h = seed ^ (8ULL * m);
+  uint64_t k = key * m;
+  k ^= k >> 47;
+  k *= m;
+  h ^= k;
+  h *= m;
+  h ^= h >> 47;
+  h *= m;
+  h ^= h >> 47;
+  return h;
+}
+
+GAL_DEVICE_INLINE uint64_t bitmask(int n) { return n >= 64 ? ~0ULL : ((1ULL << n) - 1ULL); }
+GAL_DEVICE_INLINE uint32_t blocks_in_segment(const state *s, uint32_t tree) {
+  return 1u << (s->bps_shift - tree);
+}
+GAL_DEVICE_INLINE uint64_t thread_linear_id() {
+  return (uint64_t)(threadIdx.x + blockIdx.x * blockDim.x);  // 32-bit as veb.cuh:948
+}
+
+// ------------------------------------------------------------------ vEB
+// Word layout of one tree: layer 0 (top) first; bit i of layer l word w is
+// item 64*w + i of that layer (veb.cuh:109-526, 528-1228).
+struct veb_ref {
+  uint64_t *w;
+  const veb_shape *sh;
+  uint64_t seed;
+  GAL_DEVICE_INLINE uint64_t *word(int layer, uint64_t high) const { return w + sh->off[layer] + high; }
+};
+
+GAL_DEVICE_INLINE int veb_find_next(const veb_ref &v, int layer, uint64_t high, int low) {
+  if (high >= v.sh->items[layer]) return -1;  // layer::find_next, veb.cuh:250-275
+  uint64_t b = ld_rlx(v.word(layer, high));
+  if (low == -1) return __ffsll((long long)b) - 1;
+  return __ffsll((long long)(b & ~bitmask(low + 1))) - 1;
+}
+
+GAL_DEVICE_INLINE bool veb_query(const veb_ref &v, uint64_t x) {
+  return (ld_rlx(v.word(v.sh->layers - 1, x >> 6)) >> (x & 63)) & 1ULL;
+}
+
+// veb_tree::remove (veb.cuh:737-755) plus the child re-check
+GAL_DEVICE_INLINE bool veb_remove(const veb_ref &v, uint64_t x) {
+  int layer = (int)v.sh->layers - 1;
+  uint64_t high = x >> 6;
+  int low = (int)(x & 63);
+  uint64_t old = amo_and(v.word(layer, high), ~(1ULL << low));
+  if (!(old & (1ULL << low))) return false;
+  while (__popcll(old) == 1 && layer > 0) {
+    uint64_t *child = v.word(layer, high);
+    layer -= 1;
+    low = (int)(high & 63);
+    high >>= 6;
+    old = amo_and(v.word(layer, high), ~(1ULL << low));
+    if (ld_rlx(child) != 0) {  // an insert raced in: keep the summary bit
+      amo_or(v.word(layer, high), 1ULL << low);
+      break;
+    }
+  }
+  return true;
+}
+
+// veb_tree::insert_force_update (veb.cuh:775-798)
+GAL_DEVICE_INLINE bool veb_insert(const veb_ref &v, uint64_t x) {
+  int layer = (int)v.sh->layers - 1;
+  uint64_t high = x >> 6;
+  int low = (int)(x & 63);
+  uint64_t old = amo_or(v.word(layer, high), 1ULL << low);
+  if (old & (1ULL << low)) return false;
+  while (__popcll(old) == 0 && layer > 0) {
+    layer -= 1;
+    low = (int)(high & 63);
+    high >>= 6;
+    old = amo_or(v.word(layer, high), 1ULL << low);
+  }
+  return true;
+}
+
+// veb_tree::successor_thorough (veb.cuh:878-916): smallest item > q
+GAL_DEVICE_COLD uint64_t veb_successor(const veb_ref &v, uint64_t q) {
+  const int bottom = (int)v.sh->layers - 1;
+  uint64_t high = q >> 6;
+  int low = (int)(q & 63);
+  int layer = bottom;
+  for (;;) {
+    for (;;) {
+      if (veb_find_next(v, layer, high, low) != -1) break;
+      if (layer == 0) return FAIL;
+      layer -= 1;
+      low = (int)(high & 63);
+      high >>= 6;
+    }
+    while (layer != bottom) {
+      low = veb_find_next(v, layer, high, low);
+      if (low == -1) break;
+      layer += 1;
+      high = (high << 6) + (uint64_t)low;
+      low = -1;
+    }
+    low = veb_find_next(v, layer, high, low);
+    if (low != -1) return (high << 6) + (uint64_t)low;
+  }
+}
+
+// veb_tree::lock_offset (veb.cuh:918-937)
+GAL_DEVICE_INLINE uint64_t veb_lock_offset(const veb_ref &v, uint64_t start) {
+  if (veb_query(v, start) && veb_remove(v, start)) return start;
+  for (;;) {
+    start = veb_successor(v, start);
+    if (start == FAIL) return FAIL;
+    if (veb_remove(v, start)) return start;
+  }
+}
+
+// veb_tree::malloc_first (veb.cuh:979-991)
+GAL_DEVICE_COLD uint64_t veb_malloc_first(const veb_ref &v) {
+  for (int a = 0; a < VEB_ATTEMPTS; a++) {
+    uint64_t o = veb_lock_offset(v, 0);
+    if (o != FAIL) return o;
+  }
+  return FAIL;
+}
+
+// veb_tree::find_random_valid_index (veb.cuh:946-977)
+GAL_DEVICE_COLD uint64_t veb_find_random(const veb_ref &v, uint64_t tid) {
+  const uint64_t U = v.sh->items[v.sh->layers - 1];
+  uint64_t h1 = murmur64a_u64(tid, v.seed);
+  uint64_t h2 = murmur64a_u64(tid, h1);
+  for (uint64_t a = 0; a < (uint64_t)VEB_ATTEMPTS; a++) {
+    uint64_t start = (h1 + a * h2) % U;
+    if (veb_query(v, start)) return start;
+    uint64_t idx = veb_successor(v, start);
+    if (idx != FAIL) return idx;
+  }
+  return veb_successor(v, 0);
+}
+
+// veb_tree::find_first_valid_index (veb.cuh:940-944): smallest listed id
+GAL_DEVICE_INLINE uint64_t veb_find_first(const veb_ref &v) {
+  if (veb_query(v, 0)) return 0;
+  return veb_successor(v, 0);
+}
+
+GAL_DEVICE_INLINE int cfc64(uint64_t b) {  // alloc_utils.cuh:440-453
+  int p = __popcll(b);
+  if (p == 0 || p == 64) return p;
+  return __ffsll((long long)~b) - 1;
+}
+
+GAL_DEVICE_INLINE void veb_rollback(const veb_ref &v, uint64_t start_block, uint64_t nbits) {
+  const int bottom = (int)v.sh->layers - 1;  // layer::rollback, veb.cuh:305-321
+  while (nbits > 64) {
+    amo_or(v.word(bottom, start_block), ~0ULL);
+    nbits -= 64;
+    start_block++;
+  }
+  amo_or(v.word(bottom, start_block), bitmask((int)nbits));
+}
+
+// layer::gather_multiple (veb.cuh:323-452) on the bottom layer: claims a run
+// ending in the trailing ones of a word, scanning words from the top down.
+GAL_DEVICE_COLD uint64_t veb_gather_run(const veb_ref &v, uint64_t needed) {
+  const int bottom = (int)v.sh->layers - 1;
+  uint64_t sb = v.sh->nwords[bottom] - 1;
+  while (sb != 0) {
+    uint64_t n = needed;
+    uint64_t *w = v.word(bottom, sb);
+    int c = cfc64(ld_rlx(w));
+    if (c == 0) {
+      sb -= 1;
+      continue;
+    }
+    if ((uint64_t)c >= n) {
+      uint64_t acq = bitmask((int)n) << (c - (int)n);
+      uint64_t got = amo_and(w, ~acq);
+      if ((uint64_t)__popcll(got & acq) == n) return sb * 64 + (uint64_t)(c - (int)n);
+      amo_or(w, acq & got);
+      continue;
+    }
+    uint64_t got = amo_and(w, ~bitmask(c));
+    if (__popcll(got & bitmask(c)) != c) {
+      amo_or(w, got & bitmask(c));
+      continue;
+    }
+    n -= (uint64_t)c;
+    bool ok = true;
+    while (n > 64) {
+      if (sb == 0) {  // run would leave the arena (the reference indexes word -1)
+        veb_rollback(v, 1, needed - n);
+        return FAIL;
+      }
+      sb--;
+      uint64_t full = amo_and(v.word(bottom, sb), 0ULL);
+      if (__popcll(full) != 64) {
+        amo_or(v.word(bottom, sb), full);
+        veb_rollback(v, sb + 1, needed - n);
+        ok = false;
+        break;
+      }
+      n -= 64;
+    }
+    if (!ok) continue;
+    if (sb == 0) {
+      veb_rollback(v, 1, needed - n);
+      return FAIL;
+    }
+    sb--;
+    uint64_t fmask = bitmask((int)n) << (64 - n);
+    uint64_t fb = amo_and(v.word(bottom, sb), ~fmask);
+    if ((uint64_t)__popcll(fb & fmask) == n) return sb * 64 + 64 - n;
+    amo_or(v.word(bottom, sb), fmask & fb);
+    veb_rollback(v, sb + 1, needed - n);
+  }
+  return FAIL;
+}
+
+// veb_tree::gather_multiple (veb.cuh:1160-1196)
+GAL_DEVICE_COLD uint64_t veb_gather_multiple(const veb_ref &v, uint64_t n) {
+  uint64_t found = veb_gather_run(v, n);
+  if (found == FAIL) return FAIL;
+  uint64_t lo = found;
+  for (int i = (int)v.sh->layers - 2; i >= 0; i--) {
+    uint64_t hi = (lo + n - 1) / 64 + 1;
+    lo = lo / 64;
+    n = hi - lo;
+    for (uint64_t wb = lo; wb < lo + n; wb++)
+      if (ld_rlx(v.word(i + 1, wb)) == 0) amo_and(v.word(i, wb / 64), ~(1ULL << (wb % 64)));
+  }
+  return found;
+}
+
+// veb_tree::return_multiple (veb.cuh:1198-1218, layer form veb.cuh:495-523)
+GAL_DEVICE_COLD void veb_return_multiple(const veb_ref &v, uint64_t start, uint64_t n) {
+  const int bottom = (int)v.sh->layers - 1;
+  uint64_t bi = start / 64;
+  int bs = (int)(start % 64);
+  uint64_t left = n;
+  while (left + (uint64_t)bs > 64) {
+    int add = 64 - bs;
+    amo_or(v.word(bottom, bi), bitmask(add) << bs);
+    bs = 0;
+    bi++;
+    left -= (uint64_t)add;
+  }
+  amo_or(v.word(bottom, bi), bitmask((int)left) << bs);
+  uint64_t lo = start;
+  for (int i = bottom - 1; i >= 0; i--) {
+    uint64_t hi = (lo + n - 1) / 64 + 1;
+    lo = lo / 64;
+    n = hi - lo;
+    for (uint64_t wb = lo; wb < lo + n; wb++)
+      if (__popcll(ld_rlx(v.word(i + 1, wb))) == 64) amo_or(v.word(i, wb / 64), 1ULL << (wb % 64));
+  }
+}
+
+GAL_DEVICE_INLINE veb_ref seg_tree(const state *s) { return veb_ref{s->seg_tree, &s->veb, s->seed}; }
+GAL_DEVICE_INLINE veb_ref sub_tree(const state *s, uint32_t t) {
+  return veb_ref{s->sub_trees + (uint64_t)t * s->veb.words, &s->veb, s->seed + t};
+}
+
+// ------------------------------------------------------------------ locks
+GAL_DEVICE_INLINE bool try_lock(const state *s, uint32_t bit) {
+  return (atomicOr(s->locks, 1u << bit) & (1u << bit)) == 0;  // gallatin.cuh:1513-1519
+}
+GAL_DEVICE_INLINE void unlock(const state *s, uint32_t bit) {
+  __threadfence();
+  atomicAnd(s->locks, ~(1u << bit));
+}
+
+// ------------------------------------------------------------------ table
+// alloc_table::setup_segment (memory_table.cuh:746-818)
+GAL_DEVICE_COLD bool setup_segment(const state *s, uint64_t seg, uint32_t tree) {
+  if (cas16(&s->tree_ids[seg], FREE_TREE, (uint16_t)tree) != FREE_TREE) return false;
+  uint32_t nb = blocks_in_segment(s, tree);
+  uint32_t *q = s->queues + (seg << s->bps_shift);
+  for (uint32_t i = 0; i < nb; i++) q[i] = NOBLK;
+  __threadfence();
+  atomicExch(&s->qc[seg], 0u);
+  atomicExch(&s->qfc[seg], 0u);
+  atomicExch(&s->fqfc[seg], 0u);
+  atomicExch(&s->active[seg], (int)nb - 1);
+  return true;
+}
+
+// Gallatin::gather_new_segment (gallatin.cuh:1465-1510)
+GAL_DEVICE_COLD int64_t gather_new_segment(const state *s, uint32_t tree) {
+  uint64_t seg = veb_malloc_first(seg_tree(s));
+  if (seg == FAIL) return -1;
+  if (!setup_segment(s, seg, tree)) {
+    set_error(s, GAL_DEV_ERR_SEGMENT_SETUP);
+    return -1;
+  }
+  __threadfence();
+  veb_insert(sub_tree(s, tree), seg);
+  __threadfence();
+  return (int64_t)seg;
+}
+
+// alloc_table::get_block (memory_table.cuh:915-993)
+GAL_DEVICE_COLD uint32_t get_block(const state *s, uint64_t seg, uint32_t tree, bool &last) {
+  last = false;
+  int ac = atomicSub(&s->active[seg], 1);
+  if (ac < 0) {
+    atomicAdd(&s->active[seg], 1);
+    return NOBLK;
+  }
+  __threadfence();
+  if (ld_rlx(&s->tree_ids[seg]) != (uint16_t)tree) {
+    atomicAdd(&s->active[seg], 1);
+    __threadfence();
+    return NOBLK;
+  }
+  uint32_t nb = blocks_in_segment(s, tree);
+  uint32_t pos = atomicAdd(&s->qc[seg], 1u);
+  uint32_t blk;
+  if (pos < nb) {
+    blk = (uint32_t)(seg << s->bps_shift) + pos;
+  } else {
+    uint32_t *e = s->queues + (seg << s->bps_shift) + (pos % nb);
+    blk = atomicExch(e, NOBLK);
+    for (uint32_t i = 0; blk == NOBLK && i < s->spin_limit; i++) {  // a return still in flight
+      backoff(i);
+      blk = atomicExch(e, NOBLK);
+    }
+    if (blk == NOBLK) {
+      set_error(s, GAL_DEV_ERR_NULL_QUEUE);
+      return NOBLK;
+    }
+  }
+  atomicExch(&s->mwords[blk], (unsigned long long)tree << 32);  // Block::init_malloc
+  if (ac == 0) last = true;
+  return blk;
+}
+
+// Gallatin::request_new_block_from_tree (gallatin.cuh:1525-1631)
+GAL_DEVICE_COLD uint32_t request_block(const state *s, uint32_t tree, uint64_t tid) {
+  uint32_t spins = 0;
+  int gather_fails = 0;
+  for (;;) {
+    veb_ref sub = sub_tree(s, tree);
+    uint64_t seg = s->policy == GAL_POLICY_LOWEST ? veb_find_first(sub) : veb_find_random(sub, tid);
+    if (seg == FAIL) {
+      if (try_lock(s, tree)) {
+        int64_t got = gather_new_segment(s, tree);
+        unlock(s, tree);
+        if (got < 0) {
+          // segment tree empty: nothing a retry by this thread alone changes
+          if (++gather_fails >= GATHER_RETRIES) return NOBLK;
+          backoff(gather_fails);
+          continue;
+        }
+        seg = (uint64_t)got;
+      } else {
+        if (++spins > s->spin_limit) {
+          set_error(s, GAL_DEV_ERR_TIMEOUT);
+          return NOBLK;
+        }
+        backoff(spins);
+        continue;
+      }
+    }
+    bool last = false;
+    uint32_t blk = get_block(s, seg, tree, last);
+    if (last) {
+      veb_remove(sub, seg);
+      if (try_lock(s, tree)) {
+        gather_new_segment(s, tree);
+        unlock(s, tree);
+      }
+      __threadfence();
+    }
+    if (blk != NOBLK) return blk;
+    if (++spins > s->spin_limit) {
+      set_error(s, GAL_DEV_ERR_TIMEOUT);
+      return NOBLK;
+    }
+  }
+}
+
+// Gallatin::return_block (gallatin.cuh:1637-1726) with reserve_segment_slot,
+// finalize_free_queue and finish_freeing_block (memory_table.cuh:906-910,1158-1241)
+GAL_DEVICE_COLD void return_block(const state *s, uint32_t blk) {
+  uint64_t seg = blk >> s->bps_shift;
+  uint16_t tree = ld_rlx(&s->tree_ids[seg]);
+  if (tree >= s->num_trees) {
+    set_error(s, GAL_DEV_ERR_BAD_FREE);
+    return;
+  }
+  uint32_t nb = blocks_in_segment(s, tree);
+  uint32_t pos = atomicAdd(&s->qfc[seg], 1u);
+  uint32_t live = pos % nb;
+  atomicExch(s->queues + (seg << s->bps_shift) + live, blk);
+  __threadfence();
+  for (uint32_t i = 0; atomicCAS(&s->fqfc[seg], pos, pos + 1) != pos; i++) {
+    if (i >= s->spin_limit) {
+      set_error(s, GAL_DEV_ERR_TIMEOUT);
+      break;
+    }
+    backoff(i);
+  }
+  // re-register at the 10% crossing (gallatin.cuh:1646): live/nb >= 0.1 and
+  // (live-1)/nb < 0.1 in doubles; for the power-of-two nb used here that is
+  // 10*live > nb >= 10*(live-1) with live-1 taken as unsigned (live 0 never).
+  if (live != 0 && 10ull * live > nb && 10ull * (live - 1) < nb) {
+    veb_insert(sub_tree(s, tree), seg);
+    __threadfence();
+  }
+  int rid = atomicAdd(&s->active[seg], 1);
+  bool release = false;
+  if ((uint32_t)(rid + 2) == nb) {  // all_blocks_free: rid == nb - 2
+    release = atomicCAS(&s->active[seg], (int)nb - 1, -1) == (int)nb - 1;
+  }
+  __threadfence();
+  if (release) {
+    veb_remove(sub_tree(s, tree), seg);
+    __threadfence();
+    if (cas16(&s->tree_ids[seg], tree, FREE_TREE) != tree) set_error(s, GAL_DEV_ERR_SEGMENT_SETUP);
+    __threadfence();
+    veb_insert(seg_tree(s), seg);
+  }
+}
+
+// Block::block_free_multiple + reset_free + free_block (block.cuh:87-98,200-212,
+// gallatin.cuh:1732-1766)
+GAL_DEVICE_INLINE void credit_frees(const state *s, uint32_t blk, uint32_t n) {
+  uint32_t old = atomicAdd(&s->fctr[blk], n);
+  if (old + n == SLICES_PER_BLOCK) {
+    atomicExch(&s->fctr[blk], 0u);
+    __threadfence();
+    return_block(s, blk);
+  } else if (old + n > SLICES_PER_BLOCK) {
+    set_error(s, GAL_DEV_ERR_BAD_FREE);
+  }
+}
+
+// Gallatin::free_offset (gallatin.cuh:1774-1827): team by block, one atomic
+GAL_DEVICE_INLINE void free_block_slices(const state *s, uint32_t blk) {
+  uint32_t active = __activemask();
+  uint32_t team = __match_any_sync(active, blk);
+  if ((int)lane_id() == __ffs(team) - 1) credit_frees(s, blk, (uint32_t)__popc(team));
+}
+
+// ------------------------------------------------------------------ pinned slots
+// per_size_pinned_blocks::get_valid_block_index (shared_block_storage.cuh:119-134)
+GAL_DEVICE_INLINE uint32_t pick_slot(const state *s, uint32_t tree) {
+  const uint32_t n = s->slot_count[tree];
+  const uint32_t *slots = s->slots + s->slot_base[tree];
+  uint32_t smid = s->smid_override >= 0 ? (uint32_t)s->smid_override : sm_id();
+  int my = (int)(smid % n);
+  int original = my;
+  int counter = 0;
+  while (ld_rlx(&slots[my]) == NOBLK && my != original - 1) {
+    my = (my + 1) % (int)n;
+    if (++counter >= SLOT_PROBE_LIMIT) break;
+  }
+  return (uint32_t)my;
+}
+
+// Gallatin::replace_block (gallatin.cuh:1083-1138)
+GAL_DEVICE_COLD bool replace_block(const state *s, uint32_t tree, uint32_t slot, uint32_t blk,
+                                   uint64_t tid) {
+  uint32_t *sp = s->slots + s->slot_base[tree] + slot;
+  if (atomicCAS(sp, blk, NOBLK) != blk) return true;
+  __threadfence();
+  uint32_t nb = request_block(s, tree, tid);
+  if (nb == NOBLK) return false;
+  __threadfence();
+  if (atomicCAS(sp, NOBLK, nb) != NOBLK) {
+    set_error(s, GAL_DEV_ERR_SLOT_SWAP);
+    credit_frees(s, nb, SLICES_PER_BLOCK);  // hand the unused block back
+    return false;
+  }
+  return true;
+}
+
+// Gallatin::boot_block (gallatin.cuh:726-787)
+GAL_DEVICE_COLD bool boot_block(const state *s, uint32_t tree, uint32_t slot, uint64_t tid) {
+  if (slot >= s->slot_count[tree]) return false;
+  uint32_t blk = request_block(s, tree, tid);
+  if (blk == NOBLK) return false;
+  if (ld_rlx(&s->tree_ids[blk >> s->bps_shift]) != tree) return false;
+  return atomicCAS(s->slots + s->slot_base[tree] + slot, NOBLK, blk) == NOBLK;
+}
+
+// ------------------------------------------------------------------ addresses
+GAL_DEVICE_INLINE char *slice_ptr(const state *s, uint32_t blk, uint64_t idx, uint32_t tree) {
+  uint64_t seg = blk >> s->bps_shift;
+  uint64_t q = blk & ((1u << s->bps_shift) - 1u);
+  return s->memory + (seg << s->seg_shift) + (((q << 12) + idx) << (s->min_shift + tree));
+}
+
+// ------------------------------------------------------------------ malloc tiers
+// Gallatin::malloc_slice_allocation (gallatin.cuh:865-1078): warp team per
+// size class, one atomicAdd on the pinned block per team.
+GAL_DEVICE_INLINE void *malloc_slices(const state *s, uint32_t tree, uint32_t count) {
+  const uint32_t lane = lane_id();
+  const uint64_t tid = thread_linear_id();
+  for (int attempt = 0; attempt < SLICE_ATTEMPTS; attempt++) {
+    const uint32_t active = __activemask();
+    const uint32_t team = __match_any_sync(active, tree);
+    const int leader = __ffs(team) - 1;
+    const int last = 31 - __clz(team);
+    const uint32_t lt = lanemask_lt();
+    uint32_t slot = 0, blk = NOBLK;
+    if ((int)lane == leader) {
+      slot = pick_slot(s, tree);
+      blk = ld_rlx(s->slots + s->slot_base[tree] + slot);
+    }
+    slot = __shfl_sync(active, slot, leader);
+    blk = __shfl_sync(active, blk, leader);
+    // teams whose slot was empty retry; the rest carry on with mask `live`
+    const uint32_t live = __ballot_sync(active, blk != NOBLK);
+    if (blk == NOBLK) continue;
+
+    uint32_t prefix, total;
+    if (__all_sync(live, count == 1)) {
+      prefix = (uint32_t)__popc(team & lt);
+      total = (uint32_t)__popc(team);
+    } else {  // big slices: counts are powers of two up to one block
+      prefix = 0;
+      total = 0;
+      for (uint32_t c = 1; c <= SLICES_PER_BLOCK; c <<= 1) {
+        uint32_t b = __ballot_sync(live, count == c) & team;
+        prefix += c * (uint32_t)__popc(b & lt);
+        total += c * (uint32_t)__popc(b);
+      }
+    }
+    unsigned long long old = 0;
+    if ((int)lane == last) old = atomicAdd(&s->mwords[blk], (unsigned long long)total);
+    old = __shfl_sync(live, old, last);
+    const uint64_t alloc = (old & 0xFFFFFFFFull) + prefix;
+    const bool start_valid = alloc <= SLICES_PER_BLOCK - 1;
+    const bool end_valid = alloc + count <= SLICES_PER_BLOCK;
+    const bool should_replace = start_valid && alloc + count > SLICES_PER_BLOCK - 1;
+    uint32_t leftover = start_valid ? (end_valid ? count - 1 : (uint32_t)(SLICES_PER_BLOCK - alloc)) : 0;
+    if (leftover) credit_frees(s, blk, leftover);  // block_correct_frees
+    const uint32_t rep = __ballot_sync(live, should_replace) & team;
+    if (rep && (int)lane == leader) replace_block(s, tree, slot, blk, tid);
+    __syncwarp(live);
+    if (start_valid && end_valid) {
+      if ((uint32_t)(old >> 32) == tree) return slice_ptr(s, blk, alloc, tree);
+      credit_frees(s, blk, 1);  // Block::check_valid failed: give the slice back
+    }
+  }
+  return nullptr;
+}
+
+// Gallatin::malloc_block_allocation (gallatin.cuh:828-861), Block::malloc_fill_block
+GAL_DEVICE_COLD void *malloc_whole_block(const state *s, uint32_t tree) {
+  const uint64_t tid = thread_linear_id();
+  for (int a = 0; a < BLOCK_ATTEMPTS; a++) {
+    uint32_t blk = request_block(s, tree, tid);
+    if (blk == NOBLK) return nullptr;
+    unsigned long long old = atomicAdd(&s->mwords[blk], (unsigned long long)SLICES_PER_BLOCK);
+    uint32_t old_count = (uint32_t)old;
+    if ((uint32_t)(old >> 32) != tree) set_error(s, GAL_DEV_ERR_BLOCK_TREE);
+    atomicAdd(&s->fctr[blk], (SLICES_PER_BLOCK - 1) - old_count);
+    if (old_count != 0) {
+      credit_frees(s, blk, 1);
+      continue;
+    }
+    return slice_ptr(s, blk, 0, tree);
+  }
+  return nullptr;
+}
+
+// Gallatin::malloc_segment_allocation (gallatin.cuh:790-826)
+GAL_DEVICE_COLD void *malloc_segment_run(const state *s, uint32_t count) {
+  for (int a = 0; a < SEGMENT_ATTEMPTS; a++) {
+    uint32_t spins = 0;
+    while (!try_lock(s, s->num_trees)) {
+      if (++spins > s->spin_limit) {
+        set_error(s, GAL_DEV_ERR_TIMEOUT);
+        return nullptr;
+      }
+      backoff(spins);
+    }
+    uint64_t idx = veb_gather_multiple(seg_tree(s), count);
+    if (idx != FAIL) {
+      if (cas16(&s->tree_ids[idx], FREE_TREE, (uint16_t)(s->num_trees + 1 + count)) != FREE_TREE)
+        set_error(s, GAL_DEV_ERR_SEGMENT_SETUP);
+      unlock(s, s->num_trees);
+      return s->memory + (idx << s->seg_shift);
+    }
+    unlock(s, s->num_trees);
+  }
+  return nullptr;
+}
+
+// Gallatin::malloc (gallatin.cuh:1186-1276)
+GAL_DEVICE_INLINE void *malloc(const state *s, uint64_t size) {
+  const uint32_t T = s->num_trees;
+  int bits = ceil_log2(size);
+  int tree = (size >> s->min_shift) == 0 ? 0 : bits - (int)s->min_shift;
+  uint32_t count = 1;
+  if (tree >= (int)T) {
+    int block_tree = bits - (int)(s->min_shift + 12);
+    if (block_tree >= 0) {
+      if (block_tree < (int)T) return malloc_whole_block(s, (uint32_t)block_tree);
+      return malloc_segment_run(s, (uint32_t)((size - 1) >> s->seg_shift) + 1);
+    }
+    count = 1u << (tree - (int)(T - 1));
+    tree = (int)T - 1;
+  }
+  return malloc_slices(s, (uint32_t)tree, count);
+}
+
+// multi-segment free (gallatin.cuh:1394-1417, 1283-1302), id reset first
+GAL_DEVICE_COLD void free_segment_run(const state *s, uint64_t seg, uint16_t tree) {
+  uint32_t count = (uint32_t)tree - s->num_trees - 1;
+  if (cas16(&s->tree_ids[seg], tree, FREE_TREE) != tree) {
+    set_error(s, GAL_DEV_ERR_BAD_FREE);
+    return;
+  }
+  __threadfence();
+  veb_return_multiple(seg_tree(s), seg, count);
+}
+
+// Gallatin::free (gallatin.cuh:1378-1461)
+GAL_DEVICE_INLINE void free(const state *s, void *ptr) {
+  uint64_t off = (uint64_t)((char *)ptr - s->memory);
+  uint64_t seg = off >> s->seg_shift;
+  if (seg >= s->num_segments) {
+    set_error(s, GAL_DEV_ERR_BAD_FREE);
+    return;
+  }
+  uint16_t tree = ld_rlx(&s->tree_ids[seg]);
+  if (tree >= s->num_trees) {
+    if (tree == FREE_TREE || tree == s->num_trees) {
+      set_error(s, GAL_DEV_ERR_BAD_FREE);
+      return;
+    }
+    free_segment_run(s, seg, tree);
+    return;
+  }
+  uint64_t in_seg = off & ((1ull << s->seg_shift) - 1ull);
+  uint32_t blk = (uint32_t)(seg << s->bps_shift) + (uint32_t)(in_seg >> (s->min_shift + tree + 12));
+  free_block_slices(s, blk);
+}
+
+// block id of a live pointer (slice or whole block), NOBLK for a segment run
+GAL_DEVICE_INLINE uint32_t block_of(const state *s, const void *ptr, uint16_t &tree_out) {
+  uint64_t off = (uint64_t)((const char *)ptr - s->memory);
+  uint64_t seg = off >> s->seg_shift;
+  uint16_t tree = seg < s->num_segments ? ld_rlx(&s->tree_ids[seg]) : FREE_TREE;
+  tree_out = tree;
+  if (tree >= s->num_trees) return NOBLK;
+  uint64_t in_seg = off & ((1ull << s->seg_shift) - 1ull);
+  return (uint32_t)(seg << s->bps_shift) + (uint32_t)(in_seg >> (s->min_shift + tree + 12));
+}
+
+// bytes a request of `size` occupies (Gallatin::get_allocated_size, gallatin.cuh:1152-1183)
+GAL_DEVICE_INLINE uint64_t allocated_size(const state *s, uint64_t size) {
+  if (size < 16) size = 16;
+  int bits = ceil_log2(size);
+  int tree = bits - (int)s->min_shift;
+  if (tree > (int)s->num_trees) {
+    int block_tree = bits - (int)(s->min_shift + 12);
+    if (block_tree > (int)s->num_trees) return (((size - 1) >> s->seg_shift) + 1) << s->seg_shift;
+  }
+  return 1ull << bits;
+}
+
+GAL_DEVICE_INLINE bool owns(const state *s, const void *p) {
+  return (uint64_t)((const char *)p - s->memory) < (s->num_segments << s->seg_shift);
+}
+
+}  // namespace gal

@@ -1,0 +1,135 @@
+"""ctypes wrapper of the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, never by the gallatin_gb300 package.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from gallatin_gb300._abi import FAIL, GalStateDims, StateView, GAL_POLICY_REFERENCE
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+FIX_GATHER_EXIT_ROLLBACK = 0x1
+# the product fixes these reference defects; parity runs against the product use them
+PRODUCT_FIXES = FIX_GATHER_EXIT_ROLLBACK
+
+_lib = None
+
+
+def build(force=False):
+    """Compile liboracle.so with gcc (no GPU, no CUDA needed)."""
+    src = os.path.join(HERE, "gal_oracle.c")
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        subprocess.check_call(["make", "-s", "-C", HERE, "liboracle.so"])
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        L.orc_create.restype = C.c_void_p
+        L.orc_create.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint64,
+                                 C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]
+        L.orc_destroy.argtypes = [C.c_void_p]
+        L.orc_boot_one_thread.argtypes = [C.c_void_p]
+        L.orc_malloc.restype = C.c_uint64
+        L.orc_malloc.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint64]
+        L.orc_free.argtypes = [C.c_void_p, C.c_uint64]
+        L.orc_replay.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint64, C.c_void_p]
+        L.orc_dims.argtypes = [C.c_void_p, C.c_void_p]
+        L.orc_export.argtypes = [C.c_void_p, C.c_void_p]
+        L.orc_import.argtypes = [C.c_void_p, C.c_void_p]
+        L.orc_gen_serial_trace.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint64,
+                                           C.c_uint64, C.c_void_p]
+        L.orc_gen_trace_log.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32,
+                                        C.c_uint32, C.c_void_p]
+        L.orc_murmur64a_u64.restype = C.c_uint64
+        L.orc_murmur64a_u64.argtypes = [C.c_uint64, C.c_uint64]
+        L.orc_arena_bytes.restype = C.c_uint64
+        L.orc_arena_bytes.argtypes = [C.c_void_p]
+        _lib = L
+    return _lib
+
+
+def gen_serial_trace(seed=7, nops=4096, malloc_pct=60, quantum=16, steps=256):
+    """The serial trace: splitmix64(seed); 60% malloc / 40% free of a random live op."""
+    ops = np.zeros(nops, dtype=np.uint64)
+    lib().orc_gen_serial_trace(seed, nops, malloc_pct, quantum, steps, ops.ctypes.data)
+    return ops
+
+
+def gen_log_trace(seed, nops, malloc_pct, lo_bits, hi_bits):
+    """Log-uniform sizes between 2^lo_bits and 2^hi_bits (see gal_oracle.c)."""
+    ops = np.zeros(nops, dtype=np.uint64)
+    lib().orc_gen_trace_log(seed, nops, malloc_pct, lo_bits, hi_bits, ops.ctypes.data)
+    return ops
+
+
+def murmur64a(key, seed):
+    return int(lib().orc_murmur64a_u64(key, seed))
+
+
+class Oracle:
+    """One allocator instance of the CPU model."""
+
+    def __init__(self, num_bytes, seed, bytes_per_segment=16 << 20, min_size=16, max_size=4096,
+                 pinned_first=128, pinned_min=4, fixes=PRODUCT_FIXES, policy=GAL_POLICY_REFERENCE,
+                 boot=True):
+        self._h = lib().orc_create(num_bytes, seed, bytes_per_segment, min_size, max_size,
+                                   pinned_first, pinned_min, fixes, policy)
+        if not self._h:
+            raise RuntimeError("orc_create failed")
+        self.bytes_per_segment = bytes_per_segment
+        if boot:
+            r = lib().orc_boot_one_thread(self._h)
+            if r != 0:
+                raise RuntimeError(f"oracle boot failed ({r})")
+
+    def close(self):
+        if self._h:
+            lib().orc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def malloc(self, size, smid=0, tid=0):
+        return int(lib().orc_malloc(self._h, size, smid, tid))
+
+    def free(self, byte_offset):
+        lib().orc_free(self._h, byte_offset)
+
+    def replay(self, ops, smid=0, tid=0):
+        ops = np.ascontiguousarray(ops, dtype=np.uint64)
+        out = np.full(len(ops), FAIL, dtype=np.uint64)
+        r = lib().orc_replay(self._h, ops.ctypes.data, len(ops), smid, tid, out.ctypes.data)
+        if r != 0:
+            raise ValueError("bad trace")
+        return out
+
+    def dims(self):
+        d = GalStateDims()
+        lib().orc_dims(self._h, C.byref(d))
+        return d
+
+    def export(self):
+        sv = StateView(self.dims())
+        v = sv.cview()
+        lib().orc_export(self._h, C.byref(v))
+        sv.pull(v)
+        return sv
+
+    def load(self, sv: StateView):
+        v = sv.cview()
+        lib().orc_import(self._h, C.byref(v))
+
+    @property
+    def arena_bytes(self):
+        return int(lib().orc_arena_bytes(self._h))

@@ -1,0 +1,87 @@
+"""Generate golden fixtures from the reference allocator's own CUDA build.
+
+Run on a machine with a GPU, after building the reference harness where the
+reference sources are (make -C oracle _ref/ref_harness.cubin):
+
+    python tests/golden/make_ref_golden.py [outdir]
+
+For every case it builds the reference's Gallatin<16 MiB, 16, 4096> on the
+device (oracle/ref_harness.cu), records the state after boot, replays a
+serial trace with one device thread and records the offsets it returned
+(pointer - arena base), the SM it ran on, and the final state.  The files
+written here are the fixtures checked by tests/test_oracle_golden.py.
+"""
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import refgpu  # noqa: E402
+from oracle.oracle import Oracle, gen_log_trace, gen_serial_trace  # noqa: E402
+
+GiB = 1 << 30
+
+
+def exhaust_trace():
+    """On 16 segments (all taken by the boot): 20,520 mallocs of 4 KiB run the
+    4 KiB class dry, 8,192 frees return two whole blocks (and their segments),
+    then 4 KiB mallocs (the emptied pinned slots stay empty), whole-block and
+    multi-segment requests that reuse the returned segments, and their frees."""
+    ops = [4096] * 20520
+    ops += [(1 << 63) | i for i in range(8192)]
+    ops += [4096] * 20
+    big = len(ops)
+    ops += [16 << 20, 8 << 20, (16 << 20) + 1, 64 << 10]
+    ops += [(1 << 63) | (big + i) for i in range(4)]
+    ops += [(32 << 20), 4096, 1 << 20]
+    return np.array(ops, dtype=np.uint64)
+
+
+CASES = [
+    # name, arena bytes, alloc seed, boot, trace builder
+    ("cfg1_serial", 2 * GiB, 42, refgpu.BOOT_ONE_THREAD, lambda: gen_serial_trace(7, 4096, 60, 16, 256)),
+    ("churn_16", 2 * GiB, 42, refgpu.BOOT_ONE_THREAD, lambda: gen_serial_trace(11, 100000, 50, 16, 1)),
+    ("churn_4k", 2 * GiB, 42, refgpu.BOOT_ONE_THREAD, lambda: gen_serial_trace(13, 60000, 50, 4096, 1)),
+    ("mixed_small", 2 * GiB, 42, refgpu.BOOT_ONE_THREAD, lambda: gen_serial_trace(19, 40000, 52, 16, 256)),
+    ("tiers", 16 * GiB, 42, refgpu.BOOT_ONE_THREAD, lambda: gen_log_trace(17, 3000, 55, 4, 26)),
+    ("exhaust_4k", 256 << 20, 42, refgpu.BOOT_ONE_THREAD, exhaust_trace),
+    ("cfg1_racy_boot", 2 * GiB, 42, refgpu.BOOT_RACY, lambda: gen_serial_trace(7, 4096, 60, 16, 256)),
+]
+
+
+def main():
+    out_dir = sys.argv[1] if len(sys.argv) > 1 else os.path.dirname(os.path.abspath(__file__))
+    only = set(sys.argv[2:])
+    os.makedirs(out_dir, exist_ok=True)
+    index = {}
+    for name, nbytes, seed, boot, mk in CASES:
+        if only and name not in only:
+            continue
+        t0 = time.time()
+        ops = mk()
+        dims = Oracle(nbytes, seed, boot=False).dims()
+        ref = refgpu.RefGPU(nbytes, seed, boot)
+        boot_state = ref.export(dims)
+        offsets, smid = ref.replay(ops)
+        final_state = ref.export(dims)
+        ref.close()
+        boot_state.to_npz(os.path.join(out_dir, f"{name}.boot.npz"))
+        final_state.to_npz(os.path.join(out_dir, f"{name}.final.npz"), ops=ops, offsets=offsets,
+                           smid=np.array([smid], dtype=np.uint32))
+        index[name] = {"arena_bytes": nbytes, "seed": seed, "boot": boot, "smid": smid,
+                       "nops": int(len(ops)),
+                       "mallocs": int((ops < (1 << 63)).sum()),
+                       "failed_mallocs": int(((ops < (1 << 63)) & (offsets == (1 << 64) - 1)).sum()),
+                       "seconds": round(time.time() - t0, 2)}
+        print(name, index[name], flush=True)
+    with open(os.path.join(out_dir, "index.json"), "w") as f:
+        json.dump(index, f, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()
