@@ -13,7 +13,8 @@ namespace galwl {
 
 // stats[0] mallocs ok, [1] mallocs failed, [2] payload mismatches, [3] frees
 __device__ __forceinline__ void warp_count(unsigned long long *ctr, bool flag) {
-  unsigned mask = __activemask();
+  unsigned mask;
+  asm volatile("activemask.b32 %0;" : "=r"(mask));  // read once, where written
   unsigned b = __ballot_sync(mask, flag);
   int leader = __ffs(mask) - 1;
   if ((int)(threadIdx.x & 31) == leader && b) atomicAdd(ctr, (unsigned long long)__popc(b));

@@ -1,0 +1,142 @@
+// gal_batch.cuh — CTA-level aggregation of allocation requests (the batched form).
+//
+// A CTA collects its threads' requests, ranks them per size class in shared
+// memory, and one thread per class claims the whole run of slices with a single
+// atomicAdd on the pinned block's malloc word (the per-thread path needs one
+// atomic per warp team).  Frees are combined per block through a shared-memory
+// hash so each touched block gets one free-counter atomic per CTA.
+//
+// Both entry points must be reached by every thread of the CTA (they contain
+// __syncthreads); threads without work pass has_request = false / ptr = nullptr.
+// Requests that the aggregated path cannot serve (whole blocks, segment runs,
+// multi-slice sizes, or a claim that ran out of attempts) fall back to the
+// per-thread gal::malloc / gal::free of gal_device.cuh.
+#pragma once
+
+#include "../../include/gallatin_gb300/gal_device.cuh"
+
+namespace gal {
+
+static constexpr int CTA_RUNS = 4;          // block runs a class may use per claim
+static constexpr int CTA_CLAIM_ATTEMPTS = 64;
+
+struct cta_claim_smem {
+  uint32_t count[GAL_MAX_TREES];
+  uint32_t nruns[GAL_MAX_TREES];
+  uint32_t run_blk[GAL_MAX_TREES][CTA_RUNS];
+  uint32_t run_start[GAL_MAX_TREES][CTA_RUNS];
+  uint32_t run_len[GAL_MAX_TREES][CTA_RUNS];
+};
+
+// Claim `want` slices of class `tree` for this CTA; records up to CTA_RUNS runs.
+static __device__ __noinline__ void cta_claim_class(const state *s, uint32_t tree, uint32_t want,
+                                             cta_claim_smem &sm) {
+  const uint64_t tid = thread_linear_id();
+  uint32_t assigned = 0, nruns = 0;
+  for (int attempt = 0; attempt < CTA_CLAIM_ATTEMPTS && assigned < want && nruns < CTA_RUNS;
+       attempt++) {
+    uint32_t slot = pick_slot(s, tree);
+    uint32_t blk = ld_rlx(s->slots + s->slot_base[tree] + slot);
+    if (blk == NOBLK) {
+      backoff((uint32_t)attempt);
+      continue;
+    }
+    uint32_t need = want - assigned;
+    unsigned long long old = atomicAdd(&s->mwords[blk], (unsigned long long)need);
+    uint64_t cnt = old & 0xFFFFFFFFull;
+    if (cnt >= SLICES_PER_BLOCK) continue;  // exhausted; its crosser is replacing it
+    uint32_t got = (uint32_t)min((uint64_t)need, (uint64_t)SLICES_PER_BLOCK - cnt);
+    bool crossed = cnt + need > SLICES_PER_BLOCK - 1;
+    if ((uint32_t)(old >> 32) == tree) {
+      sm.run_blk[tree][nruns] = blk;
+      sm.run_start[tree][nruns] = (uint32_t)cnt;
+      sm.run_len[tree][nruns] = got;
+      nruns++;
+      assigned += got;
+    } else {
+      credit_frees(s, blk, got);  // foreign block: give the slices back
+    }
+    if (crossed) replace_block(s, tree, slot, blk, tid);
+  }
+  sm.nruns[tree] = nruns;
+}
+
+// Returns this thread's allocation (nullptr when has_request is false).
+__device__ __forceinline__ void *cta_malloc(const state *s, uint64_t size, bool has_request,
+                                            cta_claim_smem &sm) {
+  const uint32_t T = s->num_trees;
+  if (threadIdx.x < GAL_MAX_TREES) sm.count[threadIdx.x] = 0;
+  __syncthreads();
+  int tree = -1;
+  uint32_t rank = 0;
+  if (has_request) {
+    int bits = ceil_log2(size);
+    int t = (size >> s->min_shift) == 0 ? 0 : bits - (int)s->min_shift;
+    if (t < (int)T) {
+      tree = t;
+      rank = atomicAdd(&sm.count[t], 1u);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < T && sm.count[threadIdx.x] > 0)
+    cta_claim_class(s, threadIdx.x, sm.count[threadIdx.x], sm);
+  __syncthreads();
+  void *p = nullptr;
+  bool fallback = has_request && tree < 0;
+  if (tree >= 0) {
+    uint32_t r = rank;
+    fallback = true;
+    for (uint32_t k = 0; k < sm.nruns[tree]; k++) {
+      uint32_t len = sm.run_len[tree][k];
+      if (r < len) {
+        p = slice_ptr(s, sm.run_blk[tree][k], sm.run_start[tree][k] + r, (uint32_t)tree);
+        fallback = false;
+        break;
+      }
+      r -= len;
+    }
+  }
+  if (fallback) p = gal::malloc(s, size);
+  __syncthreads();
+  return p;
+}
+
+template <int SLOTS>
+struct cta_free_smem {
+  uint32_t key[SLOTS];
+  uint32_t cnt[SLOTS];
+};
+
+// Frees `ptr` (nullptr = nothing); one free-counter atomic per distinct block.
+template <int SLOTS>
+__device__ __forceinline__ void cta_free(const state *s, void *ptr, cta_free_smem<SLOTS> &sm) {
+  for (int i = threadIdx.x; i < SLOTS; i += blockDim.x) {
+    sm.key[i] = NOBLK;
+    sm.cnt[i] = 0;
+  }
+  __syncthreads();
+  if (ptr) {
+    uint16_t tree;
+    uint32_t blk = block_of(s, ptr, tree);
+    bool placed = false;
+    if (blk != NOBLK) {
+      uint32_t h = (blk * 2654435761u) & (SLOTS - 1);
+      for (int probe = 0; probe < SLOTS; probe++) {
+        uint32_t prev = atomicCAS(&sm.key[h], NOBLK, blk);
+        if (prev == NOBLK || prev == blk) {
+          atomicAdd(&sm.cnt[h], 1u);
+          placed = true;
+          break;
+        }
+        h = (h + 1) & (SLOTS - 1);
+      }
+    }
+    if (!placed) gal::free(s, ptr);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < SLOTS; i += blockDim.x)
+    if (sm.key[i] != NOBLK) credit_frees(s, sm.key[i], sm.cnt[i]);
+  __syncthreads();
+}
+
+}  // namespace gal

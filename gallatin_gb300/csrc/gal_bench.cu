@@ -1,0 +1,502 @@
+// gal_bench.cu — workload drivers used by bench.py and the GPU tests:
+//   * mixed-size churn (16 B–4 KiB, 50% random frees per round, uint32
+//     payload written and checked), plain per-thread or CTA-batched, stream
+//     launches or one captured CUDA graph per step;
+//   * the same churn end to end through the public entry points
+//     (gal_malloc_batched / gal_free_batched) with request sizes copied from
+//     pinned host memory every round;
+//   * n threads x malloc(size) with a thread-id stamp (the reference's
+//     tests/src/global_test.cu workload);
+//   * an L2 atomic throughput probe giving the roofline denominator.
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <vector>
+
+#include "../../include/gallatin_gb300.h"
+#include "../../include/gallatin_gb300/gal_device.cuh"
+#include "churn.cuh"
+#include "gal_batch.cuh"
+
+extern "C" {
+typedef struct gal_churn_result {
+  double ms_total;           /* sum over timed steps (CUDA events)               */
+  double ms_malloc_kernels;  /* malloc-phase kernels, summed over timed steps    */
+  double ms_free_kernels;    /* free-phase kernels (incl. drain)                 */
+  uint64_t mallocs_ok, mallocs_failed, payload_mismatch, frees;
+  uint64_t malloc_launches, free_launches, other_launches;
+  uint64_t h2d_bytes, d2h_bytes; /* per timed step (e2e only)                   */
+  uint32_t error_word;
+} gal_churn_result;
+}
+
+namespace {
+
+struct plain_alloc {
+  const gal::state *s;
+  __device__ void *malloc(uint64_t n) { return gal::malloc(s, n); }
+  __device__ void free(void *p) { gal::free(s, p); }
+};
+
+constexpr int BT = 512;  // batched CTA size
+
+__global__ void k_churn_malloc_plain(const gal::state *s, void **ptrs, uint64_t base, uint64_t n,
+                                     uint32_t seed, unsigned long long *stats) {
+  plain_alloc a{s};
+  galwl::churn_malloc_body(&a, ptrs, base, n, seed, stats);
+}
+
+__global__ void k_churn_free_plain(const gal::state *s, void **ptrs, uint64_t nslots,
+                                   uint32_t round, uint32_t seed, int all,
+                                   unsigned long long *stats) {
+  plain_alloc a{s};
+  galwl::churn_free_body(&a, ptrs, nslots, round, seed, all != 0, stats);
+}
+
+// persistent, CTA-aggregated malloc phase of one round
+__global__ void __launch_bounds__(BT)
+    k_churn_malloc_batched(const gal::state *s, void **ptrs, uint64_t base, uint64_t n,
+                           uint32_t seed, unsigned long long *stats) {
+  __shared__ gal::cta_claim_smem sm;
+  for (uint64_t c = (uint64_t)blockIdx.x * BT; c < n; c += (uint64_t)gridDim.x * BT) {
+    uint64_t t = c + threadIdx.x;
+    bool has = t < n;
+    uint64_t slot = base + t;
+    uint64_t size = has ? galwl::mixed_size(slot, seed) : 0;
+    void *p = gal::cta_malloc(s, size, has, sm);
+    if (has) {
+      if (p) *(volatile uint32_t *)p = galwl::payload(slot, seed);
+      ptrs[slot] = p;
+      galwl::warp_count(&stats[0], p != nullptr);
+      galwl::warp_count(&stats[1], p == nullptr);
+    }
+  }
+}
+
+// persistent, CTA-aggregated free phase (coin flips, or everything when all)
+__global__ void __launch_bounds__(BT)
+    k_churn_free_batched(const gal::state *s, void **ptrs, uint64_t nslots, uint32_t round,
+                         uint32_t seed, int all, unsigned long long *stats) {
+  __shared__ gal::cta_free_smem<2 * BT> sm;
+  for (uint64_t c = (uint64_t)blockIdx.x * BT; c < nslots; c += (uint64_t)gridDim.x * BT) {
+    uint64_t i = c + threadIdx.x;
+    void *p = i < nslots ? ptrs[i] : nullptr;
+    bool go = p != nullptr && (all || galwl::free_coin(i, round, seed));
+    bool bad = false;
+    if (go) {
+      bad = *(volatile uint32_t *)p != galwl::payload(i, seed);
+      ptrs[i] = nullptr;
+    }
+    gal::cta_free<2 * BT>(s, go ? p : nullptr, sm);
+    if (i < nslots) {
+      galwl::warp_count(&stats[2], bad);
+      galwl::warp_count(&stats[3], go);
+    }
+  }
+}
+
+// end-to-end helpers: user-side kernels around the public batched entry points
+__global__ void k_stamp_payload(void **ptrs, uint64_t base, uint64_t n, uint32_t seed,
+                                unsigned long long *stats) {
+  uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  void *p = ptrs[base + t];
+  if (p) *(volatile uint32_t *)p = galwl::payload(base + t, seed);
+  galwl::warp_count(&stats[0], p != nullptr);
+  galwl::warp_count(&stats[1], p == nullptr);
+}
+
+__global__ void k_select_frees(void **ptrs, void **freelist, uint64_t nslots, uint32_t round,
+                               uint32_t seed, int all, unsigned long long *stats) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nslots) return;
+  void *p = ptrs[i];
+  bool go = p != nullptr && (all || galwl::free_coin(i, round, seed));
+  bool bad = false;
+  if (go) {
+    bad = *(volatile uint32_t *)p != galwl::payload(i, seed);
+    ptrs[i] = nullptr;
+  }
+  freelist[i] = go ? p : nullptr;
+  galwl::warp_count(&stats[2], bad);
+  galwl::warp_count(&stats[3], go);
+}
+
+// n threads x malloc(size) + thread-id stamp, then check + free (global_test.cu)
+__global__ void k_stamp_malloc(const gal::state *s, uint64_t n, uint64_t size, uint64_t **ptrs,
+                               unsigned long long *stats) {
+  uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= n) return;
+  uint64_t *p = (uint64_t *)gal::malloc(s, size);
+  if (p) p[0] = tid;
+  ptrs[tid] = p;
+  galwl::warp_count(&stats[0], p != nullptr);
+  galwl::warp_count(&stats[1], p == nullptr);
+}
+
+__global__ void k_stamp_free(const gal::state *s, uint64_t n, uint64_t **ptrs,
+                             unsigned long long *stats) {
+  uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= n) return;
+  uint64_t *p = ptrs[tid];
+  bool bad = false;
+  if (p) {
+    bad = p[0] != tid;
+    gal::free(s, p);
+  }
+  galwl::warp_count(&stats[2], bad);
+  galwl::warp_count(&stats[3], p != nullptr);
+}
+
+// L2 atomic probe: each thread does `iters` atomicAdd (with return) on
+// distinct words of a buffer that fits in L2 (stride keeps a warp's lanes on
+// different 32-byte sectors), or on one shared word when same_address.
+__global__ void k_atomic_probe(uint32_t *buf, uint64_t words, int iters, int same_address,
+                               uint32_t *sink) {
+  uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+  uint32_t acc = 0;
+  for (int k = 0; k < iters; k++) {
+    uint64_t idx = same_address ? 0 : ((tid * 8 + (uint64_t)k * nthreads * 8) % words);
+    acc += atomicAdd(&buf[idx], 1u);
+  }
+  if (acc == 0xFFFFFFFFu) sink[0] = acc;
+}
+
+struct churn_ctx {
+  gal_handle *h;
+  const gal::state *d;
+  uint64_t N;
+  uint32_t R, seed;
+  int batched;
+  void **ptrs;
+  unsigned long long *stats;
+  int grid_b;
+  std::vector<cudaEvent_t> ev;  // [2 per kernel]
+  int nk = 0;
+  std::vector<int> kind;        // 0 malloc, 1 free
+};
+
+void enqueue_step(churn_ctx &c, cudaStream_t st, bool capturing) {
+  const uint64_t nslots = c.N * c.R;
+  int k = 0;
+  auto mark = [&](int kind, bool begin) {
+    cudaEvent_t e = c.ev[2 * k + (begin ? 0 : 1)];
+    if (capturing)
+      cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
+    else
+      cudaEventRecord(e, st);
+    if (!begin) {
+      c.kind[k] = kind;
+      k++;
+    }
+  };
+  for (uint32_t r = 0; r <= c.R; r++) {
+    bool drain = r == c.R;
+    if (r > 0) {
+      uint64_t live = drain ? nslots : c.N * r;
+      mark(1, true);
+      if (c.batched) {
+        unsigned g = (unsigned)std::min<uint64_t>((live + BT - 1) / BT, (uint64_t)c.grid_b);
+        k_churn_free_batched<<<g, BT, 0, st>>>(c.d, c.ptrs, live, r, c.seed, drain ? 1 : 0, c.stats);
+      } else {
+        k_churn_free_plain<<<(unsigned)((live + 255) / 256), 256, 0, st>>>(c.d, c.ptrs, live, r, c.seed,
+                                                                          drain ? 1 : 0, c.stats);
+      }
+      mark(1, false);
+    }
+    if (drain) break;
+    uint64_t base = c.N * r;
+    mark(0, true);
+    if (c.batched) {
+      unsigned g = (unsigned)std::min<uint64_t>((c.N + BT - 1) / BT, (uint64_t)c.grid_b);
+      k_churn_malloc_batched<<<g, BT, 0, st>>>(c.d, c.ptrs, base, c.N, c.seed, c.stats);
+    } else {
+      k_churn_malloc_plain<<<(unsigned)((c.N + 255) / 256), 256, 0, st>>>(c.d, c.ptrs, base, c.N, c.seed,
+                                                                        c.stats);
+    }
+    mark(0, false);
+  }
+  c.nk = k;
+}
+
+#define CK(x)                                                                       \
+  do {                                                                              \
+    cudaError_t _e = (x);                                                           \
+    if (_e != cudaSuccess) {                                                        \
+      fprintf(stderr, "gallatin_gb300 bench: %s: %s\n", #x, cudaGetErrorString(_e)); \
+      rc = GAL_ERR_CUDA;                                                            \
+      goto done;                                                                    \
+    }                                                                               \
+  } while (0)
+
+}  // namespace
+
+extern "C" {
+
+/* Mixed-size churn.  One step = `rounds` x (coin frees of the live slots before
+ * every round but the first, then threads_per_round mallocs), then a drain of
+ * all live slots; every step serves the same requests.  batched: CTA-aggregated
+ * persistent kernels; use_graph: the step is one captured CUDA graph.
+ * step_ms[i]: duration of timed step i (CUDA events on the launching stream). */
+int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, uint32_t seed,
+                    int batched, int use_graph, int warmup, int steps, float *step_ms,
+                    gal_churn_result *res) {
+  if (!h || !res || !threads_per_round || !rounds || steps < 0 || warmup < 0) return GAL_ERR_ARGS;
+  int rc = GAL_OK;
+  churn_ctx c;
+  c.h = h;
+  c.d = (const gal::state *)gal_device_state(h);
+  c.N = threads_per_round;
+  c.R = rounds;
+  c.seed = seed;
+  c.batched = batched;
+  c.ptrs = nullptr;
+  c.stats = nullptr;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaStream_t st = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  const int nkern = 2 * (int)rounds + 1;
+  memset(res, 0, sizeof(*res));
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_churn_malloc_batched, BT, 0);
+  c.grid_b = sms * (per_sm > 0 ? per_sm : 1);
+  c.ev.resize(2 * nkern);
+  c.kind.resize(nkern);
+  CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  for (auto &e : c.ev) CK(cudaEventCreate(&e));
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaMalloc(&c.ptrs, threads_per_round * rounds * sizeof(void *)));
+  CK(cudaMemsetAsync(c.ptrs, 0, threads_per_round * rounds * sizeof(void *), st));
+  CK(cudaMalloc(&c.stats, 4 * sizeof(unsigned long long)));
+  if (use_graph) {
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    enqueue_step(c, st, true);
+    CK(cudaStreamEndCapture(st, &graph));
+    CK(cudaGraphInstantiate(&exec, graph, 0));
+  }
+  for (int s = 0; s < warmup + steps; s++) {
+    CK(cudaMemsetAsync(c.stats, 0, 4 * sizeof(unsigned long long), st));
+    CK(cudaStreamSynchronize(st));
+    CK(cudaEventRecord(e0, st));
+    if (use_graph)
+      CK(cudaGraphLaunch(exec, st));
+    else
+      enqueue_step(c, st, false);
+    CK(cudaEventRecord(e1, st));
+    CK(cudaEventSynchronize(e1));
+    CK(cudaGetLastError());
+    if (s >= warmup) {
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      if (step_ms) step_ms[s - warmup] = ms;
+      res->ms_total += ms;
+      for (int k = 0; k < c.nk; k++) {
+        float km = 0;
+        CK(cudaEventElapsedTime(&km, c.ev[2 * k], c.ev[2 * k + 1]));
+        if (c.kind[k] == 0) {
+          res->ms_malloc_kernels += km;
+          res->malloc_launches++;
+        } else {
+          res->ms_free_kernels += km;
+          res->free_launches++;
+        }
+      }
+      unsigned long long sv[4];
+      CK(cudaMemcpy(sv, c.stats, sizeof(sv), cudaMemcpyDeviceToHost));
+      res->mallocs_ok += sv[0];
+      res->mallocs_failed += sv[1];
+      res->payload_mismatch += sv[2];
+      res->frees += sv[3];
+    }
+  }
+  gal_last_error(h, &res->error_word);
+done:
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  for (auto &e : c.ev)
+    if (e) cudaEventDestroy(e);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (c.ptrs) cudaFree(c.ptrs);
+  if (c.stats) cudaFree(c.stats);
+  if (st) cudaStreamDestroy(st);
+  return rc;
+}
+
+/* The churn end to end through the public entry points: every round the
+ * request sizes are copied from pinned host memory (host_sizes, rounds x
+ * threads_per_round, same sizes as the device-generated workload), served by
+ * gal_malloc_batched, stamped by a user kernel; frees are selected by a user
+ * kernel and served by gal_free_batched; the step's counters are read back. */
+int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t threads_per_round,
+                        uint32_t rounds, uint32_t seed, int warmup, int steps, float *step_ms,
+                        gal_churn_result *res) {
+  if (!h || !res || !host_sizes || !threads_per_round || !rounds) return GAL_ERR_ARGS;
+  int rc = GAL_OK;
+  const uint64_t N = threads_per_round, nslots = N * rounds;
+  void **ptrs = nullptr, **freelist = nullptr;
+  uint64_t *d_sizes = nullptr;
+  unsigned long long *stats = nullptr;
+  unsigned long long hst[4];
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  memset(res, 0, sizeof(*res));
+  CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaMalloc(&ptrs, nslots * sizeof(void *)));
+  CK(cudaMalloc(&freelist, nslots * sizeof(void *)));
+  CK(cudaMalloc(&d_sizes, N * sizeof(uint64_t)));
+  CK(cudaMalloc(&stats, 4 * sizeof(unsigned long long)));
+  CK(cudaMemsetAsync(ptrs, 0, nslots * sizeof(void *), st));
+  for (int s = 0; s < warmup + steps; s++) {
+    CK(cudaStreamSynchronize(st));
+    CK(cudaEventRecord(e0, st));
+    CK(cudaMemsetAsync(stats, 0, sizeof(hst), st));
+    for (uint32_t r = 0; r <= rounds; r++) {
+      bool drain = r == rounds;
+      if (r > 0) {
+        uint64_t live = drain ? nslots : N * r;
+        k_select_frees<<<(unsigned)((live + 255) / 256), 256, 0, st>>>(ptrs, freelist, live, r, seed,
+                                                                      drain ? 1 : 0, stats);
+        int e = gal_free_batched(h, freelist, live, st);
+        if (e) { rc = e; goto done; }
+      }
+      if (drain) break;
+      CK(cudaMemcpyAsync(d_sizes, host_sizes + (uint64_t)r * N, N * sizeof(uint64_t),
+                         cudaMemcpyHostToDevice, st));
+      int e = gal_malloc_batched(h, d_sizes, N, ptrs + (uint64_t)r * N, st);
+      if (e) { rc = e; goto done; }
+      k_stamp_payload<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(ptrs, (uint64_t)r * N, N, seed, stats);
+    }
+    CK(cudaMemcpyAsync(hst, stats, sizeof(hst), cudaMemcpyDeviceToHost, st));
+    CK(cudaEventRecord(e1, st));
+    CK(cudaEventSynchronize(e1));
+    CK(cudaGetLastError());
+    if (s >= warmup) {
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      if (step_ms) step_ms[s - warmup] = ms;
+      res->ms_total += ms;
+      res->mallocs_ok += hst[0];
+      res->mallocs_failed += hst[1];
+      res->payload_mismatch += hst[2];
+      res->frees += hst[3];
+      res->malloc_launches += rounds;
+      res->free_launches += rounds;
+      res->other_launches += 2 * rounds;
+    }
+  }
+  res->h2d_bytes = nslots * sizeof(uint64_t);
+  res->d2h_bytes = sizeof(hst);
+  gal_last_error(h, &res->error_word);
+done:
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (ptrs) cudaFree(ptrs);
+  if (freelist) cudaFree(freelist);
+  if (d_sizes) cudaFree(d_sizes);
+  if (stats) cudaFree(stats);
+  if (st) cudaStreamDestroy(st);
+  return rc;
+}
+
+/* Request sizes of the churn workload, computed on the host (for e2e). */
+int gal_churn_sizes(uint64_t base_slot, uint64_t n, uint32_t seed, uint64_t *out) {
+  if (!out) return GAL_ERR_ARGS;
+  for (uint64_t i = 0; i < n; i++) out[i] = galwl::mixed_size(base_slot + i, seed);
+  return GAL_OK;
+}
+
+/* n threads x malloc(size) with a thread-id stamp, then check and free, for
+ * `rounds` rounds.  ms[0]: malloc kernels, ms[1]: free kernels (summed).
+ * stats: [0] ok [1] failed [2] stamp mismatches [3] frees. */
+int gal_bench_stamp(gal_handle *h, uint64_t n, uint64_t size, int rounds, float *ms,
+                    uint64_t *stats_out) {
+  if (!h || !ms || !stats_out || !n) return GAL_ERR_ARGS;
+  int rc = GAL_OK;
+  uint64_t **ptrs = nullptr;
+  unsigned long long *stats = nullptr;
+  cudaEvent_t a = nullptr, b = nullptr, c = nullptr;
+  const gal::state *d = (const gal::state *)gal_device_state(h);
+  unsigned grid = (unsigned)((n + 255) / 256);
+  ms[0] = ms[1] = 0;
+  CK(cudaMalloc(&ptrs, n * sizeof(void *)));
+  CK(cudaMalloc(&stats, 32));
+  CK(cudaMemset(stats, 0, 32));
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  CK(cudaEventCreate(&c));
+  for (int r = 0; r < rounds; r++) {
+    CK(cudaEventRecord(a));
+    k_stamp_malloc<<<grid, 256>>>(d, n, size, ptrs, stats);
+    CK(cudaEventRecord(b));
+    k_stamp_free<<<grid, 256>>>(d, n, ptrs, stats);
+    CK(cudaEventRecord(c));
+    CK(cudaEventSynchronize(c));
+    CK(cudaGetLastError());
+    float x = 0, y = 0;
+    CK(cudaEventElapsedTime(&x, a, b));
+    CK(cudaEventElapsedTime(&y, b, c));
+    ms[0] += x;
+    ms[1] += y;
+  }
+  CK(cudaMemcpy(stats_out, stats, 32, cudaMemcpyDeviceToHost));
+done:
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  if (c) cudaEventDestroy(c);
+  if (ptrs) cudaFree(ptrs);
+  if (stats) cudaFree(stats);
+  return rc;
+}
+
+/* L2 atomic throughput (atomicAdd.u32 with return) in atomics per second, on
+ * distinct words of a 32 MiB buffer (resident in L2) and on one word. */
+int gal_bench_atomic_peak(double *distinct_per_s, double *same_addr_per_s) {
+  if (!distinct_per_s || !same_addr_per_s) return GAL_ERR_ARGS;
+  int rc = GAL_OK;
+  uint32_t *buf = nullptr, *sink = nullptr;
+  cudaEvent_t a = nullptr, b = nullptr;
+  const uint64_t words = (32ull << 20) / 4;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const unsigned grid = (unsigned)sms * 8, block = 256;
+  const int iters = 256;
+  CK(cudaMalloc(&buf, words * 4));
+  CK(cudaMalloc(&sink, 4));
+  CK(cudaMemset(buf, 0, words * 4));
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  for (int same = 0; same < 2; same++) {
+    int it = same ? 16 : iters;
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; rep++) {
+      CK(cudaEventRecord(a));
+      k_atomic_probe<<<grid, block>>>(buf, words, it, same, sink);
+      CK(cudaEventRecord(b));
+      CK(cudaEventSynchronize(b));
+      CK(cudaGetLastError());
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, a, b));
+      if (rep > 0 && ms < best) best = ms;
+    }
+    double n = (double)grid * block * it;
+    (same ? *same_addr_per_s : *distinct_per_s) = n / (best * 1e-3);
+  }
+done:
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  if (buf) cudaFree(buf);
+  if (sink) cudaFree(sink);
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,619 @@
+// gal_lib.cu — host side of the allocator behind the C ABI of
+// include/gallatin_gb300.h, plus the kernels the library launches itself
+// (initialisation, boot, state export/import, statistics, serial replay,
+// per-thread and batched malloc/free).
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <mutex>
+#include <unordered_map>
+
+#include "../../include/gallatin_gb300.h"
+#include "../../include/gallatin_gb300/gal_device.cuh"
+#include "gal_batch.cuh"
+
+struct gal_handle {
+  int device = 0;
+  gal_config cfg{};
+  uint64_t num_bytes = 0, seed = 0;
+  gal::state st{};             // host copy of the device-resident state
+  gal::state *d_state = nullptr;
+  char *meta = nullptr;
+  size_t meta_bytes = 0;
+  char *arena = nullptr;
+  uint64_t arena_bytes = 0;
+  gal_state_dims dims{};
+};
+
+namespace {
+
+std::mutex g_mu;
+std::unordered_map<const void *, gal_handle *> g_by_state;
+gal_handle *g_global = nullptr;
+
+#define CUDA_TRY(x)                                                                   \
+  do {                                                                                \
+    cudaError_t _e = (x);                                                             \
+    if (_e != cudaSuccess) {                                                          \
+      fprintf(stderr, "gallatin_gb300: %s failed: %s\n", #x, cudaGetErrorString(_e)); \
+      return GAL_ERR_CUDA;                                                            \
+    }                                                                                 \
+  } while (0)
+
+bool is_pow2(uint64_t x) { return x && !(x & (x - 1)); }
+uint32_t log2u(uint64_t x) { return 63 - __builtin_clzll(x); }
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) & ~(a - 1); }
+
+// ---------------------------------------------------------------- kernels
+__global__ void k_init_words(unsigned long long *mwords, uint64_t nblocks, uint64_t *seg_tree,
+                             gal::veb_shape sh) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t b = i; b < nblocks; b += stride) mwords[b] = 4097ull;  // Block::init
+  for (uint32_t l = 0; l < sh.layers; l++) {
+    uint64_t items = sh.items[l];
+    for (uint64_t w = i; w < sh.nwords[l]; w += stride) {
+      uint64_t lo = w * 64;
+      uint64_t n = items > lo ? items - lo : 0;
+      seg_tree[sh.off[l] + w] = n >= 64 ? ~0ull : ((1ull << n) - 1ull);
+    }
+  }
+}
+
+// boot_shared_block_container_one_thread order (gallatin.cuh:196-221)
+__global__ void k_boot(const gal::state *s) {
+  if (threadIdx.x + blockIdx.x * blockDim.x != 0) return;
+  for (uint32_t t = 0; t < s->num_trees; t++)
+    for (uint32_t i = 0; i < s->slot_count[t]; i++)
+      if (!gal::boot_block(s, t, i, 0)) gal::set_error(s, GAL_DEV_ERR_BOOT);
+}
+
+__global__ void k_export_blocks(const gal::state *s, uint32_t *mc, uint64_t nblocks) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t b = i; b < nblocks; b += stride) {
+    unsigned long long w = s->mwords[b];
+    mc[b] = (uint32_t)(((w >> 32) << 20) + (w & 0xFFFFFFFFull));  // reference packing
+  }
+}
+
+__global__ void k_import_blocks(const gal::state *s, const uint32_t *mc, uint64_t nblocks) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t b = i; b < nblocks; b += stride)
+    s->mwords[b] = ((unsigned long long)(mc[b] >> 20) << 32) | (mc[b] & 0xFFFFFu);
+}
+
+__global__ void k_stats(const gal::state *s, gal_stats *out) {
+  __shared__ unsigned long long acc[3 + 3 * GAL_MAX_TREES];
+  const uint32_t T = s->num_trees;
+  for (int i = threadIdx.x; i < 3 + 3 * GAL_MAX_TREES; i += blockDim.x) acc[i] = 0;
+  __syncthreads();
+  const uint32_t bottom = s->veb.layers - 1;
+  const uint64_t nw = s->veb.nwords[bottom];
+  for (uint64_t w = threadIdx.x; w < nw; w += blockDim.x) {
+    atomicAdd(&acc[0], (unsigned long long)__popcll(s->seg_tree[s->veb.off[bottom] + w]));
+    for (uint32_t t = 0; t < T; t++)
+      atomicAdd(&acc[3 + GAL_MAX_TREES + t],
+                (unsigned long long)__popcll(
+                    s->sub_trees[(uint64_t)t * s->veb.words + s->veb.off[bottom] + w]));
+  }
+  for (uint64_t g = threadIdx.x; g < s->num_segments; g += blockDim.x) {
+    uint16_t id = s->tree_ids[g];
+    if (id < T) {
+      atomicAdd(&acc[3 + id], 1ull);
+      int handed = (int)gal::blocks_in_segment(s, id) - 1 - s->active[g];
+      if (handed > 0) atomicAdd(&acc[3 + 2 * GAL_MAX_TREES + id], (unsigned long long)handed);
+    } else if (id != 0xFFFF && id > T) {
+      atomicAdd(&acc[1], 1ull);
+      atomicAdd(&acc[2], (unsigned long long)(id - T - 1));
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    // longest run of free segments in the bottom layer of the segment tree
+    uint64_t best = 0, cur = 0;
+    for (uint64_t g = 0; g < s->num_segments; g++) {
+      bool f = (s->seg_tree[s->veb.off[bottom] + (g >> 6)] >> (g & 63)) & 1ull;
+      cur = f ? cur + 1 : 0;
+      if (cur > best) best = cur;
+    }
+    out->num_segments = s->num_segments;
+    out->free_segments = acc[0];
+    out->largest_free_run = best;
+    out->num_trees = T;
+    out->error_word = *s->error;
+    for (uint32_t t = 0; t < GAL_MAX_TREES; t++) {
+      out->tree_segments[t] = t < T ? acc[3 + t] : 0;
+      out->tree_listed[t] = t < T ? acc[3 + GAL_MAX_TREES + t] : 0;
+      out->tree_live_blocks[t] = t < T ? acc[3 + 2 * GAL_MAX_TREES + t] : 0;
+    }
+    out->multi_segment_allocs = acc[1];
+    out->multi_segment_segments = acc[2];
+  }
+}
+
+// one device thread replays a trace (gallatin_single_thread.cu generalised)
+__global__ void k_replay(const gal::state *s, const uint64_t *ops, uint64_t nops, uint64_t *out,
+                         uint32_t *out_smid) {
+  if (threadIdx.x + blockIdx.x * blockDim.x != 0) return;
+  out_smid[0] = gal::sm_id();
+  for (uint64_t i = 0; i < nops; i++) {
+    uint64_t op = ops[i];
+    if (op >> 63) {
+      uint64_t target = op & ~(1ull << 63);
+      if (target < i && out[target] != gal::FAIL) gal::free(s, s->memory + out[target]);
+      out[i] = gal::FAIL;
+    } else {
+      void *p = gal::malloc(s, op);
+      out[i] = p ? (uint64_t)((char *)p - s->memory) : gal::FAIL;
+    }
+  }
+}
+
+__global__ void k_malloc_per_thread(const gal::state *s, const uint64_t *sizes, uint64_t n,
+                                    void **out) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = gal::malloc(s, sizes[i]);
+}
+
+__global__ void k_free_per_thread(const gal::state *s, void *const *ptrs, uint64_t n) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  void *p = ptrs[i];
+  if (p) gal::free(s, p);
+}
+
+constexpr int BATCH_THREADS = 512;
+
+__global__ void __launch_bounds__(BATCH_THREADS)
+    k_malloc_batched(const gal::state *s, const uint64_t *sizes, uint64_t n, void **out) {
+  __shared__ gal::cta_claim_smem sm;
+  for (uint64_t base = (uint64_t)blockIdx.x * BATCH_THREADS; base < n;
+       base += (uint64_t)gridDim.x * BATCH_THREADS) {
+    uint64_t i = base + threadIdx.x;
+    bool has = i < n;
+    void *p = gal::cta_malloc(s, has ? sizes[i] : 0, has, sm);
+    if (has) out[i] = p;
+  }
+}
+
+__global__ void __launch_bounds__(BATCH_THREADS)
+    k_free_batched(const gal::state *s, void *const *ptrs, uint64_t n) {
+  __shared__ gal::cta_free_smem<2 * BATCH_THREADS> sm;
+  for (uint64_t base = (uint64_t)blockIdx.x * BATCH_THREADS; base < n;
+       base += (uint64_t)gridDim.x * BATCH_THREADS) {
+    uint64_t i = base + threadIdx.x;
+    gal::cta_free<2 * BATCH_THREADS>(s, i < n ? ptrs[i] : nullptr, sm);
+  }
+}
+
+int persistent_grid(int device) {
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_malloc_batched, BATCH_THREADS, 0);
+  if (per_sm < 1) per_sm = 1;
+  return sms * per_sm;
+}
+
+void free_handle(gal_handle *h) {
+  if (!h) return;
+  if (h->meta) cudaFree(h->meta);
+  if (h->arena) cudaFree(h->arena);
+  delete h;
+}
+
+int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot, gal_handle **out) {
+  if (!out) return GAL_ERR_ARGS;
+  *out = nullptr;
+  gal_config cfg;
+  if (cfg_in)
+    cfg = *cfg_in;
+  else
+    gal_config_default(&cfg);
+  if (!is_pow2(cfg.bytes_per_segment) || !is_pow2(cfg.min_size) || !is_pow2(cfg.max_size))
+    return GAL_ERR_ARGS;
+  if (cfg.max_size < cfg.min_size || cfg.bytes_per_segment < cfg.max_size * 4096) return GAL_ERR_ARGS;
+  if (cfg.subtree_policy > GAL_POLICY_LOWEST) return GAL_ERR_ARGS;
+  const uint32_t T = log2u(cfg.max_size) - log2u(cfg.min_size) + 1;
+  const uint64_t S = num_bytes / cfg.bytes_per_segment;
+  if (T > GAL_MAX_TREES || S == 0 || S + T + 1 >= 0xFFFF) return GAL_ERR_ARGS;
+  const uint32_t bps_shift = log2u(cfg.bytes_per_segment) - log2u(cfg.min_size) - 12;
+  const uint64_t nblocks = S << bps_shift;
+  if (nblocks >= 0xFFFFFFFFull) return GAL_ERR_ARGS;
+
+  gal_handle *h = new gal_handle();
+  h->cfg = cfg;
+  h->num_bytes = num_bytes;
+  h->seed = seed;
+  cudaGetDevice(&h->device);
+  gal::state &st = h->st;
+  st.num_segments = S;
+  st.seed = seed;
+  st.seg_shift = log2u(cfg.bytes_per_segment);
+  st.min_shift = log2u(cfg.min_size);
+  st.bps_shift = bps_shift;
+  st.num_trees = T;
+  st.policy = cfg.subtree_policy;
+  st.smid_override = cfg.smid_override;
+  st.spin_limit = cfg.spin_limit ? cfg.spin_limit : (1u << 16);
+  // pinned slots: first, halving per tree, floored (shared_block_storage.cuh:260-267)
+  uint64_t n = cfg.pinned_slots_first, total = 0;
+  for (uint32_t t = 0; t < T; t++) {
+    uint64_t c = n == 0 ? 1 : n;
+    st.slot_base[t] = (uint32_t)total;
+    st.slot_count[t] = (uint32_t)c;
+    total += c;
+    n = n / 2;
+    if (n < cfg.pinned_slots_min) n = cfg.pinned_slots_min;
+  }
+  st.total_slots = (uint32_t)total;
+  // vEB shape over S items (veb.cuh:595-649)
+  int max_height = 64 - __builtin_clzll(S);
+  st.veb.layers = (uint32_t)((max_height - 1) / 6 + 1);
+  {
+    uint64_t u = S;
+    for (uint32_t i = 0; i < st.veb.layers; i++) {
+      uint32_t l = st.veb.layers - 1 - i;
+      st.veb.items[l] = u;
+      st.veb.nwords[l] = (uint32_t)((u - 1) / 64 + 1);
+      u = (u - 1) / 64 + 1;
+    }
+    uint32_t o = 0;
+    for (uint32_t l = 0; l < st.veb.layers; l++) {
+      st.veb.off[l] = o;
+      o += st.veb.nwords[l];
+    }
+    st.veb.words = o;
+  }
+  // one metadata region
+  const size_t A = 256;
+  size_t off = 0;
+  auto carve = [&](size_t bytes) {
+    size_t o = off;
+    off = align_up(off + bytes, A);
+    return o;
+  };
+  size_t o_state = carve(sizeof(gal::state));
+  size_t o_seg = carve((size_t)st.veb.words * 8);
+  size_t o_sub = carve((size_t)T * st.veb.words * 8);
+  size_t o_ids = carve(S * 2);
+  size_t o_act = carve(S * 4), o_qc = carve(S * 4), o_qfc = carve(S * 4), o_fqfc = carve(S * 4);
+  size_t o_mw = carve(nblocks * 8), o_fc = carve(nblocks * 4), o_q = carve(nblocks * 4);
+  size_t o_slots = carve(total * 4);
+  size_t o_locks = carve(128), o_err = carve(128);
+  h->meta_bytes = off;
+  if (cudaMalloc(&h->meta, h->meta_bytes) != cudaSuccess) {
+    free_handle(h);
+    return GAL_ERR_OOM;
+  }
+  h->arena_bytes = S * cfg.bytes_per_segment;
+  if (cudaMalloc(&h->arena, h->arena_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    free_handle(h);
+    return GAL_ERR_OOM;
+  }
+  char *m = h->meta;
+  st.memory = h->arena;
+  st.seg_tree = (uint64_t *)(m + o_seg);
+  st.sub_trees = (uint64_t *)(m + o_sub);
+  st.tree_ids = (uint16_t *)(m + o_ids);
+  st.active = (int32_t *)(m + o_act);
+  st.qc = (uint32_t *)(m + o_qc);
+  st.qfc = (uint32_t *)(m + o_qfc);
+  st.fqfc = (uint32_t *)(m + o_fqfc);
+  st.mwords = (unsigned long long *)(m + o_mw);
+  st.fctr = (uint32_t *)(m + o_fc);
+  st.queues = (uint32_t *)(m + o_q);
+  st.slots = (uint32_t *)(m + o_slots);
+  st.locks = (uint32_t *)(m + o_locks);
+  st.error = (uint32_t *)(m + o_err);
+  h->d_state = (gal::state *)(m + o_state);
+
+  int rc = GAL_OK;
+  do {
+    // everything zero, then the non-zero patterns
+    if (cudaMemset(h->meta, 0, h->meta_bytes) != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
+    if (cudaMemset(st.tree_ids, 0xFF, S * 2) != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
+    if (cudaMemset(st.active, 0xFF, S * 4) != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
+    if (cudaMemset(st.queues, 0xFF, nblocks * 4) != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
+    if (cudaMemset(st.slots, 0xFF, total * 4) != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
+    k_init_words<<<1024, 256>>>(st.mwords, nblocks, st.seg_tree, st.veb);
+    if (cudaGetLastError() != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
+    if (cfg.zero_arena && cudaMemset(h->arena, 0, h->arena_bytes) != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
+    if (cudaMemcpy(h->d_state, &st, sizeof(st), cudaMemcpyHostToDevice) != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
+    if (boot) {
+      k_boot<<<1, 1>>>(h->d_state);
+      if (cudaGetLastError() != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
+    }
+    if (cudaDeviceSynchronize() != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
+    uint32_t err = 0;
+    if (cudaMemcpy(&err, st.error, 4, cudaMemcpyDeviceToHost) != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
+    if (err) { rc = GAL_ERR_DEVICE; break; }
+  } while (0);
+  if (rc != GAL_OK) {
+    free_handle(h);
+    return rc;
+  }
+  // dims of the state view
+  h->dims.num_segments = S;
+  h->dims.num_trees = T;
+  h->dims.blocks_per_segment = 1u << bps_shift;
+  h->dims.veb_layers = st.veb.layers;
+  h->dims.veb_words = st.veb.words;
+  h->dims.total_slots = (uint32_t)total;
+  for (uint32_t t = 0; t < T; t++) h->dims.slot_counts[t] = st.slot_count[t];
+  {
+    std::lock_guard<std::mutex> g(g_mu);
+    g_by_state[h->d_state] = h;
+  }
+  *out = h;
+  return GAL_OK;
+}
+
+int push_state(gal_handle *h) {
+  CUDA_TRY(cudaMemcpy(h->d_state, &h->st, sizeof(h->st), cudaMemcpyHostToDevice));
+  return GAL_OK;
+}
+
+unsigned grid_for(uint64_t n, unsigned block) {
+  uint64_t g = (n + block - 1) / block;
+  if (g == 0) g = 1;
+  if (g > 0x7FFFFFFFull) g = 0x7FFFFFFFull;
+  return (unsigned)g;
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+int gal_config_default(gal_config *cfg) {
+  if (!cfg) return GAL_ERR_ARGS;
+  cfg->bytes_per_segment = 16ull << 20;
+  cfg->min_size = 16;
+  cfg->max_size = 4096;
+  cfg->smid_override = -1;
+  cfg->subtree_policy = GAL_POLICY_REFERENCE;
+  cfg->pinned_slots_first = 128;
+  cfg->pinned_slots_min = 4;
+  cfg->zero_arena = 1;
+  cfg->spin_limit = 1u << 16;  // x backoff capped at 4 us: ~0.27 s per wait at most
+  return GAL_OK;
+}
+
+int gal_create(uint64_t num_bytes, uint64_t seed, const gal_config *cfg, gal_handle **out) {
+  return build(num_bytes, seed, cfg, true, out);
+}
+
+int gal_create_unbooted(uint64_t num_bytes, uint64_t seed, const gal_config *cfg, gal_handle **out) {
+  return build(num_bytes, seed, cfg, false, out);
+}
+
+int gal_destroy(gal_handle *h) {
+  if (!h) return GAL_ERR_ARGS;
+  cudaDeviceSynchronize();
+  {
+    std::lock_guard<std::mutex> g(g_mu);
+    g_by_state.erase(h->d_state);
+    if (g_global == h) g_global = nullptr;
+  }
+  free_handle(h);
+  return GAL_OK;
+}
+
+gal_handle *gal_handle_of(const void *device_state) {
+  std::lock_guard<std::mutex> g(g_mu);
+  auto it = g_by_state.find(device_state);
+  return it == g_by_state.end() ? nullptr : it->second;
+}
+
+void *gal_device_state(gal_handle *h) { return h ? (void *)h->d_state : nullptr; }
+void *gal_arena_base(gal_handle *h) { return h ? (void *)h->arena : nullptr; }
+uint64_t gal_arena_bytes(gal_handle *h) { return h ? h->arena_bytes : 0; }
+
+int gal_get_stats(gal_handle *h, gal_stats *out) {
+  if (!h || !out) return GAL_ERR_ARGS;
+  gal_stats *d = nullptr;
+  CUDA_TRY(cudaMalloc(&d, sizeof(gal_stats)));
+  k_stats<<<1, 1024>>>(h->d_state, d);
+  cudaError_t e = cudaMemcpy(out, d, sizeof(gal_stats), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return GAL_ERR_CUDA;
+  out->metadata_bytes = h->meta_bytes;
+  return GAL_OK;
+}
+
+int gal_print_stats(gal_handle *h) {
+  gal_stats s;
+  int rc = gal_get_stats(h, &s);
+  if (rc) return rc;
+  printf("\nGallatin (GB300) usage stats:\n");
+  printf("Segment tree sees %llu/%llu segments available, largest free run %llu\n",
+         (unsigned long long)s.free_segments, (unsigned long long)s.num_segments,
+         (unsigned long long)s.largest_free_run);
+  for (uint32_t t = 0; t < s.num_trees; t++)
+    printf("Tree %u: size %llu, owns %llu segments, lists %llu, %llu blocks handed out\n", t,
+           (unsigned long long)(h->cfg.min_size << t), (unsigned long long)s.tree_segments[t],
+           (unsigned long long)s.tree_listed[t], (unsigned long long)s.tree_live_blocks[t]);
+  printf("Multi-segment allocations: %llu covering %llu segments\n",
+         (unsigned long long)s.multi_segment_allocs, (unsigned long long)s.multi_segment_segments);
+  printf("Allocator is using %llu bytes of metadata, error word 0x%x\n",
+         (unsigned long long)s.metadata_bytes, s.error_word);
+  return GAL_OK;
+}
+
+int gal_last_error(gal_handle *h, uint32_t *bits) {
+  if (!h || !bits) return GAL_ERR_ARGS;
+  CUDA_TRY(cudaMemcpy(bits, h->st.error, 4, cudaMemcpyDeviceToHost));
+  return GAL_OK;
+}
+
+int gal_clear_error(gal_handle *h) {
+  if (!h) return GAL_ERR_ARGS;
+  CUDA_TRY(cudaMemset(h->st.error, 0, 8 + 4 * sizeof(uint64_t)));
+  return GAL_OK;
+}
+
+int gal_error_info(gal_handle *h, uint64_t *out4) {
+  if (!h || !out4) return GAL_ERR_ARGS;
+  CUDA_TRY(cudaMemcpy(out4, h->st.error + 2, 4 * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+  return GAL_OK;
+}
+
+int gal_state_dims_get(gal_handle *h, gal_state_dims *out) {
+  if (!h || !out) return GAL_ERR_ARGS;
+  *out = h->dims;
+  return GAL_OK;
+}
+
+int gal_export_state(gal_handle *h, const gal_state_view *v) {
+  if (!h || !v) return GAL_ERR_ARGS;
+  const gal::state &st = h->st;
+  const uint64_t S = st.num_segments, nb = S << st.bps_shift, W = st.veb.words, T = st.num_trees;
+  CUDA_TRY(cudaDeviceSynchronize());
+  CUDA_TRY(cudaMemcpy(v->seg_tree_words, st.seg_tree, W * 8, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(v->sub_tree_words, st.sub_trees, T * W * 8, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(v->tree_ids, st.tree_ids, S * 2, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(v->active_counts, st.active, S * 4, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(v->queue_counters, st.qc, S * 4, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(v->queue_free_counters, st.qfc, S * 4, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(v->final_queue_free_counters, st.fqfc, S * 4, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(v->free_counters, st.fctr, nb * 4, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(v->queues, st.queues, nb * 4, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(v->slots, st.slots, (uint64_t)st.total_slots * 4, cudaMemcpyDeviceToHost));
+  uint32_t *d_mc = nullptr;
+  CUDA_TRY(cudaMalloc(&d_mc, nb * 4));
+  k_export_blocks<<<1024, 256>>>(h->d_state, d_mc, nb);
+  cudaError_t e = cudaMemcpy(v->malloc_counters, d_mc, nb * 4, cudaMemcpyDeviceToHost);
+  cudaFree(d_mc);
+  if (e != cudaSuccess) return GAL_ERR_CUDA;
+  uint32_t locks = 0, err = 0;
+  CUDA_TRY(cudaMemcpy(&locks, st.locks, 4, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(&err, st.error, 4, cudaMemcpyDeviceToHost));
+  ((gal_state_view *)v)->locks = locks;
+  ((gal_state_view *)v)->error_word = err;
+  return GAL_OK;
+}
+
+int gal_import_state(gal_handle *h, const gal_state_view *v) {
+  if (!h || !v) return GAL_ERR_ARGS;
+  const gal::state &st = h->st;
+  const uint64_t S = st.num_segments, nb = S << st.bps_shift, W = st.veb.words, T = st.num_trees;
+  CUDA_TRY(cudaDeviceSynchronize());
+  CUDA_TRY(cudaMemcpy(st.seg_tree, v->seg_tree_words, W * 8, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(st.sub_trees, v->sub_tree_words, T * W * 8, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(st.tree_ids, v->tree_ids, S * 2, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(st.active, v->active_counts, S * 4, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(st.qc, v->queue_counters, S * 4, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(st.qfc, v->queue_free_counters, S * 4, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(st.fqfc, v->final_queue_free_counters, S * 4, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(st.fctr, v->free_counters, nb * 4, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(st.queues, v->queues, nb * 4, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(st.slots, v->slots, (uint64_t)st.total_slots * 4, cudaMemcpyHostToDevice));
+  uint32_t *d_mc = nullptr;
+  CUDA_TRY(cudaMalloc(&d_mc, nb * 4));
+  cudaError_t e = cudaMemcpy(d_mc, v->malloc_counters, nb * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    k_import_blocks<<<1024, 256>>>(h->d_state, d_mc, nb);
+    e = cudaDeviceSynchronize();
+  }
+  cudaFree(d_mc);
+  if (e != cudaSuccess) return GAL_ERR_CUDA;
+  uint32_t locks = v->locks;
+  CUDA_TRY(cudaMemcpy(st.locks, &locks, 4, cudaMemcpyHostToDevice));
+  return GAL_OK;
+}
+
+int gal_set_smid_override(gal_handle *h, int32_t smid) {
+  if (!h) return GAL_ERR_ARGS;
+  h->st.smid_override = smid;
+  h->cfg.smid_override = smid;
+  return push_state(h);
+}
+
+int gal_set_policy(gal_handle *h, uint32_t policy) {
+  if (!h || policy > GAL_POLICY_LOWEST) return GAL_ERR_ARGS;
+  h->st.policy = policy;
+  h->cfg.subtree_policy = policy;
+  return push_state(h);
+}
+
+int gal_init(uint64_t num_bytes, uint64_t seed, const gal_config *cfg) {
+  {
+    std::lock_guard<std::mutex> g(g_mu);
+    if (g_global) return GAL_ERR_STATE;
+  }
+  gal_handle *h = nullptr;
+  int rc = gal_create(num_bytes, seed, cfg, &h);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> g(g_mu);
+  g_global = h;
+  return GAL_OK;
+}
+
+int gal_teardown(void) {
+  gal_handle *h;
+  {
+    std::lock_guard<std::mutex> g(g_mu);
+    h = g_global;
+  }
+  if (!h) return GAL_ERR_STATE;
+  return gal_destroy(h);
+}
+
+gal_handle *gal_global(void) {
+  std::lock_guard<std::mutex> g(g_mu);
+  return g_global;
+}
+
+int gal_replay_trace(gal_handle *h, const uint64_t *ops, uint64_t nops, uint64_t *out_offsets,
+                     uint32_t *out_smid, void *stream) {
+  if (!h || !ops || !out_offsets || !out_smid) return GAL_ERR_ARGS;
+  k_replay<<<1, 1, 0, (cudaStream_t)stream>>>(h->d_state, ops, nops, out_offsets, out_smid);
+  CUDA_TRY(cudaGetLastError());
+  return GAL_OK;
+}
+
+int gal_malloc_per_thread(gal_handle *h, const uint64_t *sizes, uint64_t n, void **out, void *stream) {
+  if (!h || (n && (!sizes || !out))) return GAL_ERR_ARGS;
+  if (!n) return GAL_OK;
+  k_malloc_per_thread<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(h->d_state, sizes, n, out);
+  CUDA_TRY(cudaGetLastError());
+  return GAL_OK;
+}
+
+int gal_free_per_thread(gal_handle *h, void *const *ptrs, uint64_t n, void *stream) {
+  if (!h || (n && !ptrs)) return GAL_ERR_ARGS;
+  if (!n) return GAL_OK;
+  k_free_per_thread<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(h->d_state, ptrs, n);
+  CUDA_TRY(cudaGetLastError());
+  return GAL_OK;
+}
+
+int gal_malloc_batched(gal_handle *h, const uint64_t *sizes, uint64_t n, void **out, void *stream) {
+  if (!h || (n && (!sizes || !out))) return GAL_ERR_ARGS;
+  if (!n) return GAL_OK;
+  unsigned g = grid_for(n, BATCH_THREADS);
+  unsigned p = (unsigned)persistent_grid(h->device);
+  k_malloc_batched<<<g < p ? g : p, BATCH_THREADS, 0, (cudaStream_t)stream>>>(h->d_state, sizes, n, out);
+  CUDA_TRY(cudaGetLastError());
+  return GAL_OK;
+}
+
+int gal_free_batched(gal_handle *h, void *const *ptrs, uint64_t n, void *stream) {
+  if (!h || (n && !ptrs)) return GAL_ERR_ARGS;
+  if (!n) return GAL_OK;
+  unsigned g = grid_for(n, BATCH_THREADS);
+  unsigned p = (unsigned)persistent_grid(h->device);
+  k_free_batched<<<g < p ? g : p, BATCH_THREADS, 0, (cudaStream_t)stream>>>(h->d_state, ptrs, n);
+  CUDA_TRY(cudaGetLastError());
+  return GAL_OK;
+}
+
+}  // extern "C"

@@ -134,6 +134,8 @@ int gal_destroy(gal_handle *h);
 
 /* Device pointer to the allocator object (what a Gallatin<>* points to). */
 void *gal_device_state(gal_handle *h);
+/* Host handle that owns a device allocator object (NULL if none). */
+gal_handle *gal_handle_of(const void *device_state);
 /* Device pointer to the first byte of the arena (alloc_table::memory,
  * memory_table.cuh:255). */
 void *gal_arena_base(gal_handle *h);
@@ -149,6 +151,8 @@ int gal_print_stats(gal_handle *h);
  * on invariant breaks (gallatin.cuh:87). */
 int gal_last_error(gal_handle *h, uint32_t *out_bits);
 int gal_clear_error(gal_handle *h);
+/* First recorded error: out4 = {site, value a, value b, recorded flag}. */
+int gal_error_info(gal_handle *h, uint64_t *out4);
 
 /* State view export/import (no reference counterpart: test and drain-check
  * support, SURVEY-style "snapshot"). */

@@ -33,7 +33,9 @@
 #ifndef GAL_DEVICE_INLINE
 #define GAL_DEVICE_INLINE __device__ __forceinline__
 #endif
-#define GAL_DEVICE_COLD __device__ __noinline__
+// cold paths stay out of line (register pressure of the hot path); static so
+// the header can be included by several translation units
+#define GAL_DEVICE_COLD static __device__ __noinline__
 
 namespace gal {
 
@@ -96,6 +98,14 @@ GAL_DEVICE_INLINE uint32_t lane_id() {
   asm volatile("mov.u32 %0, %%laneid;" : "=r"(r));
   return r;
 }
+// Mask of the lanes executing here.  Read through volatile asm: the
+// __activemask() builtin may be re-evaluated by the compiler at a later,
+// divergent use site, which splits a warp team across convergence groups.
+GAL_DEVICE_INLINE uint32_t active_lanes() {
+  uint32_t m;
+  asm volatile("activemask.b32 %0;" : "=r"(m));
+  return m;
+}
 GAL_DEVICE_INLINE uint32_t lanemask_lt() {
   uint32_t r;
   asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(r));
@@ -134,6 +144,26 @@ GAL_DEVICE_INLINE uint16_t cas16(uint16_t *p, uint16_t cmp, uint16_t val) {
   return (uint16_t)atomicCAS((unsigned short *)p, (unsigned short)cmp, (unsigned short)val);
 }
 GAL_DEVICE_INLINE void set_error(const state *s, uint32_t bits) { atomicOr(s->error, bits); }
+// error word plus the first error's site and two values (error[2..9] as 4 u64:
+// site, a, b, taken) for gal_error_info
+GAL_DEVICE_COLD void set_error_info(const state *s, uint32_t bits, uint64_t site, uint64_t a,
+                                    uint64_t b) {
+  atomicOr(s->error, bits);
+  unsigned long long *info = (unsigned long long *)(s->error + 2);
+  if (atomicCAS(&info[3], 0ull, 1ull) == 0ull) {
+    info[0] = site;
+    info[1] = a;
+    info[2] = b;
+    __threadfence();
+  }
+}
+enum : uint64_t {
+  SITE_RETURN_BAD_TREE = 1,
+  SITE_FREE_OVERFLOW = 2,
+  SITE_FREE_OUTSIDE = 3,
+  SITE_FREE_FREE_SEGMENT = 4,
+  SITE_FREE_RUN_TWICE = 5,
+};
 GAL_DEVICE_INLINE void backoff(uint32_t i) { __nanosleep(i < 8 ? 32u << i : 4096u); }
 
 // ceil(log2(x)) for x > 0, 0 for x == 0 (alloc_utils.cuh:382-398)
@@ -244,7 +274,9 @@ GAL_DEVICE_COLD uint64_t veb_successor(const veb_ref &v, uint64_t q) {
       low = -1;
     }
     low = veb_find_next(v, layer, high, low);
-    if (low != -1) return (high << 6) + (uint64_t)low;
+    // only a bottom-layer hit is an item; a summary word refilled by a racing
+    // insert is searched again from the top of the loop
+    if (low != -1 && layer == bottom) return (high << 6) + (uint64_t)low;
   }
 }
 
@@ -308,7 +340,11 @@ GAL_DEVICE_INLINE void veb_rollback(const veb_ref &v, uint64_t start_block, uint
 GAL_DEVICE_COLD uint64_t veb_gather_run(const veb_ref &v, uint64_t needed) {
   const int bottom = (int)v.sh->layers - 1;
   uint64_t sb = v.sh->nwords[bottom] - 1;
+  // every pass either moves down a word or retries one that changed under it;
+  // bound the retries so heavy interference ends in a clean failure
+  uint64_t budget = 8ull * v.sh->nwords[bottom] + 1024;
   while (sb != 0) {
+    if (budget-- == 0) return FAIL;
     uint64_t n = needed;
     uint64_t *w = v.word(bottom, sb);
     int c = cfc64(ld_rlx(w));
@@ -520,6 +556,7 @@ GAL_DEVICE_COLD uint32_t request_block(const state *s, uint32_t tree, uint64_t t
       set_error(s, GAL_DEV_ERR_TIMEOUT);
       return NOBLK;
     }
+    backoff(spins);
   }
 }
 
@@ -529,7 +566,7 @@ GAL_DEVICE_COLD void return_block(const state *s, uint32_t blk) {
   uint64_t seg = blk >> s->bps_shift;
   uint16_t tree = ld_rlx(&s->tree_ids[seg]);
   if (tree >= s->num_trees) {
-    set_error(s, GAL_DEV_ERR_BAD_FREE);
+    set_error_info(s, GAL_DEV_ERR_BAD_FREE, SITE_RETURN_BAD_TREE, blk, tree);
     return;
   }
   uint32_t nb = blocks_in_segment(s, tree);
@@ -575,13 +612,14 @@ GAL_DEVICE_INLINE void credit_frees(const state *s, uint32_t blk, uint32_t n) {
     __threadfence();
     return_block(s, blk);
   } else if (old + n > SLICES_PER_BLOCK) {
-    set_error(s, GAL_DEV_ERR_BAD_FREE);
+    set_error_info(s, GAL_DEV_ERR_BAD_FREE, SITE_FREE_OVERFLOW, blk,
+                   ((uint64_t)old << 32) | n);
   }
 }
 
 // Gallatin::free_offset (gallatin.cuh:1774-1827): team by block, one atomic
 GAL_DEVICE_INLINE void free_block_slices(const state *s, uint32_t blk) {
-  uint32_t active = __activemask();
+  uint32_t active = active_lanes();
   uint32_t team = __match_any_sync(active, blk);
   if ((int)lane_id() == __ffs(team) - 1) credit_frees(s, blk, (uint32_t)__popc(team));
 }
@@ -642,18 +680,15 @@ GAL_DEVICE_INLINE void *malloc_slices(const state *s, uint32_t tree, uint32_t co
   const uint32_t lane = lane_id();
   const uint64_t tid = thread_linear_id();
   for (int attempt = 0; attempt < SLICE_ATTEMPTS; attempt++) {
-    const uint32_t active = __activemask();
+    const uint32_t active = active_lanes();
     const uint32_t team = __match_any_sync(active, tree);
     const int leader = __ffs(team) - 1;
     const int last = 31 - __clz(team);
     const uint32_t lt = lanemask_lt();
-    uint32_t slot = 0, blk = NOBLK;
-    if ((int)lane == leader) {
-      slot = pick_slot(s, tree);
-      blk = ld_rlx(s->slots + s->slot_base[tree] + slot);
-    }
-    slot = __shfl_sync(active, slot, leader);
-    blk = __shfl_sync(active, blk, leader);
+    // every lane of a team reads the same slot words in the same instruction
+    // (one broadcast transaction), so the team needs no leader branch here
+    const uint32_t slot = pick_slot(s, tree);
+    const uint32_t blk = __shfl_sync(active, ld_rlx(s->slots + s->slot_base[tree] + slot), leader);
     // teams whose slot was empty retry; the rest carry on with mask `live`
     const uint32_t live = __ballot_sync(active, blk != NOBLK);
     if (blk == NOBLK) continue;
@@ -755,7 +790,7 @@ GAL_DEVICE_INLINE void *malloc(const state *s, uint64_t size) {
 GAL_DEVICE_COLD void free_segment_run(const state *s, uint64_t seg, uint16_t tree) {
   uint32_t count = (uint32_t)tree - s->num_trees - 1;
   if (cas16(&s->tree_ids[seg], tree, FREE_TREE) != tree) {
-    set_error(s, GAL_DEV_ERR_BAD_FREE);
+    set_error_info(s, GAL_DEV_ERR_BAD_FREE, SITE_FREE_RUN_TWICE, seg, tree);
     return;
   }
   __threadfence();
@@ -767,13 +802,13 @@ GAL_DEVICE_INLINE void free(const state *s, void *ptr) {
   uint64_t off = (uint64_t)((char *)ptr - s->memory);
   uint64_t seg = off >> s->seg_shift;
   if (seg >= s->num_segments) {
-    set_error(s, GAL_DEV_ERR_BAD_FREE);
+    set_error_info(s, GAL_DEV_ERR_BAD_FREE, SITE_FREE_OUTSIDE, off, 0);
     return;
   }
   uint16_t tree = ld_rlx(&s->tree_ids[seg]);
   if (tree >= s->num_trees) {
     if (tree == FREE_TREE || tree == s->num_trees) {
-      set_error(s, GAL_DEV_ERR_BAD_FREE);
+      set_error_info(s, GAL_DEV_ERR_BAD_FREE, SITE_FREE_FREE_SEGMENT, off, tree);
       return;
     }
     free_segment_run(s, seg, tree);

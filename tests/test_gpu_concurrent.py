@@ -1,0 +1,179 @@
+"""Concurrent correctness of the CUDA allocator on the GPU (through the C ABI).
+
+Invariants (no reference counterpart gives exact offsets here):
+  * every live allocation is non-null, aligned to its size class inside a
+    16 MiB-aligned segment, and no two live ranges overlap;
+  * stamped payloads read back intact (the reference's tid-stamp test and its
+    exchange-check churn, tests/src/global_test.cu, global_churn.cu);
+  * the device error word stays clear;
+  * a full drain leaves every block's counters balanced.
+"""
+import numpy as np
+import pytest
+
+from gallatin_gb300._abi import GAL_DEV_ERR_BAD_FREE
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def G():
+    import gallatin_gb300
+    return gallatin_gb300
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as t
+    return t
+
+
+SEG = 16 << 20
+
+
+def _class_bytes(sizes):
+    """Bytes a request occupies (Gallatin::get_allocated_size, gallatin.cuh:1152)."""
+    s = np.maximum(sizes, 16)
+    c = 1 << np.ceil(np.log2(s)).astype(np.int64)
+    big = s > SEG
+    c[big] = ((s[big] - 1) // SEG + 1) * SEG
+    return c
+
+
+def _alignment(sizes):
+    """Slices: their size; 8-32 KiB (runs of 4 KiB slices): 4 KiB; whole blocks:
+    the block size; segment runs: 16 MiB."""
+    c = _class_bytes(sizes)
+    a = c.copy()
+    a[(sizes > 4096) & (sizes <= 32768)] = 4096
+    a[sizes > SEG] = SEG
+    return a
+
+
+def _check_no_overlap(ptrs, sizes, base):
+    order = np.argsort(ptrs)
+    p, n, a = ptrs[order], _class_bytes(sizes)[order], _alignment(sizes)[order]
+    assert (p[1:] >= p[:-1] + n[:-1]).all(), "live allocations overlap"
+    assert (((p - base) % a) == 0).all(), "misaligned allocation"
+
+
+def test_stamp_1m_threads_16B(G):
+    """Config-1 concurrent case: 1,048,576 threads x malloc(16), tid stamp, check, free."""
+    g = G.Gallatin.generate_on_device(2 << 30, 42)
+    try:
+        ms, st = g.bench_stamp(1 << 20, 16, rounds=3)
+        assert st[0] == 3 << 20 and st[1] == 0, st
+        assert st[2] == 0 and st[3] == 3 << 20, st
+        assert g.error_word() == 0, g.error_info()
+    finally:
+        g.close()
+
+
+@pytest.mark.parametrize("batched", [False, True])
+def test_mixed_sizes_no_overlap(G, torch, batched):
+    n = 1 << 20
+    rng = np.random.default_rng(1 if batched else 2)
+    sizes = (2 ** rng.uniform(4, 12, n)).astype(np.int64)
+    g = G.Gallatin.generate_on_device(4 << 30, 42)
+    try:
+        d_sizes = torch.from_numpy(sizes).cuda()
+        d_ptrs = torch.zeros(n, dtype=torch.int64, device="cuda")
+        (g.malloc_batched if batched else g.malloc_per_thread)(d_sizes, d_ptrs)
+        torch.cuda.synchronize()
+        ptrs = d_ptrs.cpu().numpy()
+        assert (ptrs != 0).all()
+        _check_no_overlap(ptrs, sizes, g.arena_base)
+        (g.free_batched if batched else g.free_per_thread)(d_ptrs)
+        torch.cuda.synchronize()
+        assert g.error_word() == 0, g.error_info()
+        sv = g.export()
+        # every counted free matched a claimed slice: no free counter above 4096
+        assert (sv.free_counters <= 4096).all()
+    finally:
+        g.close()
+
+
+def test_block_and_segment_tiers_no_overlap(G, torch):
+    n = 4096
+    rng = np.random.default_rng(3)
+    sizes = (2 ** rng.uniform(13, 27, n)).astype(np.int64)  # 8 KiB .. 128 MiB
+    sizes[sizes > (64 << 20)] = 40 << 20
+    g = G.Gallatin.generate_on_device(64 << 30, 7)
+    try:
+        d_sizes = torch.from_numpy(sizes).cuda()
+        d_ptrs = torch.zeros(n, dtype=torch.int64, device="cuda")
+        g.malloc_per_thread(d_sizes, d_ptrs)
+        torch.cuda.synchronize()
+        ptrs = d_ptrs.cpu().numpy()
+        ok = ptrs != 0
+        assert ok.mean() > 0.5
+        _check_no_overlap(ptrs[ok], sizes[ok], g.arena_base)
+        g.free_per_thread(d_ptrs)
+        torch.cuda.synchronize()
+        assert g.error_word() == 0, g.error_info()
+        st = g.stats()
+        assert st.multi_segment_allocs == 0
+    finally:
+        g.close()
+
+
+@pytest.mark.parametrize("batched", [False, True])
+def test_churn_payloads(G, batched):
+    """Mixed 16 B - 4 KiB churn, 50% random frees per round, payload checked."""
+    g = G.Gallatin.generate_on_device(16 << 30, 42)
+    try:
+        N, R = 1 << 18, 6
+        ms, r = g.bench_churn(N, R, 1, batched, batched, 1, 2)
+        assert r.mallocs_ok == 2 * N * R and r.mallocs_failed == 0
+        assert r.payload_mismatch == 0
+        assert r.frees == r.mallocs_ok
+        assert r.error_word == 0
+    finally:
+        g.close()
+
+
+def test_exhaustion_returns_null_then_recovers(G, torch):
+    """Tiny arena: 4 KiB class runs dry, frees give whole segments back, and
+    whole-block requests are served again."""
+    g = G.Gallatin.generate_on_device(512 << 20, 42)
+    try:
+        n = 200_000
+        d_sizes = torch.full((n,), 4096, dtype=torch.int64, device="cuda")
+        d_ptrs = torch.zeros(n, dtype=torch.int64, device="cuda")
+        g.malloc_per_thread(d_sizes, d_ptrs)
+        torch.cuda.synchronize()
+        ptrs = d_ptrs.cpu().numpy()
+        got = (ptrs != 0).sum()
+        assert 0 < got < n                     # ran out of memory, returned nullptr
+        _check_no_overlap(ptrs[ptrs != 0], np.full(got, 4096), g.arena_base)
+        assert g.error_word() == 0, g.error_info()
+        g.free_per_thread(d_ptrs)
+        torch.cuda.synchronize()
+        st = g.stats()
+        assert st.free_segments > 0
+        big = torch.full((8,), 8 << 20, dtype=torch.int64, device="cuda")
+        bp = torch.zeros(8, dtype=torch.int64, device="cuda")
+        g.malloc_per_thread(big, bp)
+        torch.cuda.synchronize()
+        assert (bp.cpu().numpy() != 0).sum() >= 1
+        g.free_per_thread(bp)
+        torch.cuda.synchronize()
+        assert g.error_word() == 0, g.error_info()
+    finally:
+        g.close()
+
+
+def test_double_free_is_reported_not_trapped(G, torch):
+    g = G.Gallatin.generate_on_device(2 << 30, 42)
+    try:
+        big = torch.full((1,), 20 << 20, dtype=torch.int64, device="cuda")
+        bp = torch.zeros(1, dtype=torch.int64, device="cuda")
+        g.malloc_per_thread(big, bp)
+        g.free_per_thread(bp)
+        g.free_per_thread(bp)  # second free of a multi-segment run
+        torch.cuda.synchronize()
+        assert g.error_word() & GAL_DEV_ERR_BAD_FREE
+        g.clear_error()
+        assert g.error_word() == 0, g.error_info()
+    finally:
+        g.close()

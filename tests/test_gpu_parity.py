@@ -1,0 +1,119 @@
+"""Serial parity of the CUDA allocator (through the C ABI) on the GPU.
+
+A trace replayed by one device thread must return the reference build's
+offsets byte for byte and leave the same state, word for word:
+  * against the fixtures recorded from the reference's own CUDA build
+    (tests/golden/, see make_ref_golden.py), with the pinned-slot SM id set to
+    the one the reference ran on;
+  * against the CPU oracle (product mode) on further random traces, at the SM
+    id this run landed on.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from gallatin_gb300._abi import FAIL, GAL_POLICY_LOWEST, StateView
+from oracle.oracle import PRODUCT_FIXES, Oracle, gen_log_trace, gen_serial_trace
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+INDEX = json.load(open(os.path.join(GOLD, "index.json")))
+
+
+@pytest.fixture(scope="module")
+def G():
+    import gallatin_gb300
+    return gallatin_gb300
+
+
+def _golden(name):
+    boot, _ = StateView.from_npz(os.path.join(GOLD, f"{name}.boot.npz"))
+    final, z = StateView.from_npz(os.path.join(GOLD, f"{name}.final.npz"))
+    return boot, final, z["ops"], z["offsets"], int(z["smid"][0])
+
+
+@pytest.mark.parametrize("name", sorted(INDEX))
+def test_serial_trace_matches_reference_build(G, name):
+    meta = INDEX[name]
+    boot, final, ops, offsets, smid = _golden(name)
+    one_thread = meta["boot"] == 1
+    g = G.Gallatin.generate_on_device(meta["arena_bytes"], meta["seed"], boot=one_thread,
+                                      smid_override=smid)
+    try:
+        if one_thread:
+            assert g.export().diff(boot) == [], "boot state differs from the reference build"
+        else:
+            g.load(boot)
+        out, _ = g.replay(ops)
+        np.testing.assert_array_equal(out, offsets)
+        assert g.export().diff(final) == [], "final state differs from the reference build"
+        assert g.error_word() == 0
+    finally:
+        g.close()
+
+
+TRACES = [
+    ("serial_s101", 2 << 30, lambda: gen_serial_trace(101, 20000, 55, 16, 256)),
+    ("serial_s202_16", 2 << 30, lambda: gen_serial_trace(202, 30000, 50, 16, 1)),
+    ("log_4_15", 2 << 30, lambda: gen_log_trace(303, 20000, 52, 4, 15)),
+    ("log_4_26", 16 << 30, lambda: gen_log_trace(404, 4000, 55, 4, 26)),
+    ("log_big_small_arena", 1 << 30, lambda: gen_log_trace(505, 3000, 60, 10, 24)),
+]
+
+
+@pytest.mark.parametrize("name,nbytes,mk", TRACES, ids=[t[0] for t in TRACES])
+def test_serial_trace_matches_oracle(G, name, nbytes, mk):
+    ops = mk()
+    g = G.Gallatin.generate_on_device(nbytes, 42)
+    try:
+        out, smid = g.replay(ops)
+        o = Oracle(nbytes, 42, fixes=PRODUCT_FIXES)
+        np.testing.assert_array_equal(out, o.replay(ops, smid=smid))
+        assert g.export().diff(o.export()) == []
+        assert g.error_word() == 0
+    finally:
+        g.close()
+
+
+def test_lowest_policy_matches_oracle(G):
+    ops = gen_serial_trace(606, 30000, 50, 4096, 1)
+    g = G.Gallatin.generate_on_device(2 << 30, 9, subtree_policy=GAL_POLICY_LOWEST)
+    try:
+        out, smid = g.replay(ops)
+        o = Oracle(2 << 30, 9, fixes=PRODUCT_FIXES, policy=GAL_POLICY_LOWEST)
+        np.testing.assert_array_equal(out, o.replay(ops, smid=smid))
+        assert g.export().diff(o.export()) == []
+    finally:
+        g.close()
+
+
+@pytest.mark.parametrize("geom", [(64 << 20, 16, 4096), (64 << 20, 128, 16384), (16 << 20, 128, 4096)])
+def test_other_geometries_match_oracle(G, geom):
+    seg, mn, mx = geom
+    ops = gen_log_trace(707, 8000, 55, 4, 20)
+    g = G.Gallatin.generate_on_device(4 << 30, 3, bytes_per_segment=seg, min_size=mn, max_size=mx)
+    try:
+        out, smid = g.replay(ops)
+        o = Oracle(4 << 30, 3, bytes_per_segment=seg, min_size=mn, max_size=mx, fixes=PRODUCT_FIXES)
+        np.testing.assert_array_equal(out, o.replay(ops, smid=smid))
+        assert g.export().diff(o.export()) == []
+    finally:
+        g.close()
+
+
+def test_state_roundtrip_export_import(G):
+    g = G.Gallatin.generate_on_device(2 << 30, 42)
+    try:
+        g.replay(gen_serial_trace(11, 5000, 60, 16, 256))
+        sv = g.export()
+        h = G.Gallatin.generate_on_device(2 << 30, 42, boot=False)
+        try:
+            h.load(sv)
+            assert h.export().diff(sv) == []
+        finally:
+            h.close()
+    finally:
+        g.close()
