@@ -58,6 +58,15 @@ def parse():
     p.add_argument("--threads-per-round", type=int, default=N_PER_ROUND)
     p.add_argument("--rounds", type=int, default=ROUNDS)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--arena-gib", type=int, default=ARENA >> 30)
+    p.add_argument("--slots", type=int, default=0,
+                   help="pinned slots per size class for the batched form (0: one per SM)")
+    p.add_argument("--unlocked", type=int, default=16,
+                   help="batched form: classes with fewer blocks per segment gather without the lock")
+    p.add_argument("--segment-mib", type=int, default=64, help="batched form: segment size")
+    p.add_argument("--free-mode", default="cta", choices=["cta", "warp"],
+                   help="batched form: frees combined per CTA (shared-memory hash) or per warp team")
+    p.add_argument("--quick", action="store_true", help="headline batched steps only (profiling)")
     return p.parse_args()
 
 
@@ -147,9 +156,10 @@ def sum_over_ranks(x, world):
     return float(t.item())
 
 
-def read_profile_traffic():
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "churn_malloc_batched_16GiB.md")
+def read_profile_traffic(kernel):
+    """Per-launch DRAM bytes of `kernel` at the full workload, from the committed
+    ncu summary profiles/<kernel>.md (line `traffic_bytes_per_launch: N`)."""
+    path = os.path.join(ROOT, "profiles", kernel + ".md")
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -241,26 +251,27 @@ def main():
     import gallatin_gb300 as G
 
     N, R = args.threads_per_round, args.rounds
-    g = G.Gallatin.generate_on_device(ARENA, ALLOC_SEED)
+    arena = args.arena_gib << 30
+    # the batched form runs with its tuned knobs; the plain per-thread form with
+    # the reference's defaults (128 pinned slots halving to 4)
+    tuned = dict(pinned_slots_first=args.slots, pinned_slots_min=args.slots if args.slots else 0,
+                 gather_unlocked_below=args.unlocked, bytes_per_segment=args.segment_mib << 20)
+    g = G.Gallatin.generate_on_device(arena, ALLOC_SEED, **tuned)
 
     # one probe step: a workload that does not fit would run the out-of-memory
     # retry paths for minutes, so stop here instead
-    _, probe = g.bench_churn(N, R, SEED, batched=True, use_graph=False, warmup=0, steps=1)
+    mode = 1 | (2 if args.free_mode == "cta" else 0)
+    _, probe = g.bench_churn(N, R, SEED, batched=mode, use_graph=False, warmup=0, steps=1)
     if probe.mallocs_failed or probe.payload_mismatch or probe.error_word:
         print(json.dumps({"metric": METRIC, "error": "probe step failed", "probe": probe.as_dict()}))
         sys.exit(3)
-
-    # plain per-thread path (stream launches), for the batched/plain ratio
-    plain_ms, plain = g.bench_churn(N, R, SEED, batched=False, use_graph=False,
-                                    warmup=1, steps=max(1, args.steps // 2))
-    plain_v = (plain.mallocs_ok + plain.frees) / (plain.ms_total / 1e3)
 
     # headline: batched + graph
     barrier(world)
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         t0 = time.time()
-        ms, res = g.bench_churn(N, R, SEED, batched=True, use_graph=True,
+        ms, res = g.bench_churn(N, R, SEED, batched=mode, use_graph=True,
                                 warmup=args.warmup, steps=args.steps)
         wall = time.time() - t0
     torch.cuda.synchronize()
@@ -268,6 +279,12 @@ def main():
     secs = max_over_ranks(res.ms_total / 1e3, world)
     ops = sum_over_ranks(float(res.mallocs_ok + res.frees), world)
     value = ops / secs
+    if args.quick:
+        g.close()
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "ops/s", "quick": True,
+                              "result": res.as_dict()}))
+        return
 
     # end to end through the public C ABI with host-resident request sizes
     sizes = torch.empty(N * R, dtype=torch.int64, pin_memory=True)
@@ -280,6 +297,16 @@ def main():
     barrier(world)
     esecs = max_over_ranks(eres.ms_total / 1e3, world)
     e2e_v = sum_over_ranks(float(eres.mallocs_ok + eres.frees), world) / esecs
+    del sizes
+
+    # p50/p99 per-request latency (clock64 cycles) of one full-concurrency round
+    def lat(a, batched):
+        mc, fc = a.bench_latency(N, SEED + 7, batched)
+        return {"malloc_p50_cycles": float(np.percentile(mc, 50)),
+                "malloc_p99_cycles": float(np.percentile(mc, 99)),
+                "free_p50_cycles": float(np.percentile(fc, 50)),
+                "free_p99_cycles": float(np.percentile(fc, 99))}
+    latency = {"requests": N, "batched": lat(g, True)}
 
     # roofline: the dominant kernel (malloc or free phase), 1 algorithmic atomic per op
     distinct, same = G.atomic_peak()
@@ -288,13 +315,23 @@ def main():
         kern, ms_k, n_launch, units = ("k_churn_malloc_batched", res.ms_malloc_kernels,
                                        res.malloc_launches, res.mallocs_ok)
     else:
-        kern, ms_k, n_launch, units = ("k_churn_free_batched", res.ms_free_kernels,
-                                       res.free_launches, res.frees)
+        kern, ms_k, n_launch, units = (
+            "k_churn_free_batched" if args.free_mode == "cta" else "k_churn_free_plain",
+            res.ms_free_kernels, res.free_launches, res.frees)
     avg_launch_s = ms_k / 1e3 / n_launch
     achieved = (units / n_launch) / avg_launch_s
-    traffic = read_profile_traffic()
+    traffic = read_profile_traffic(kern)
     errors = g.error_word()
     g.close()
+
+    # plain per-thread path on the reference's default knobs, stream launches
+    gp = G.Gallatin.generate_on_device(arena, ALLOC_SEED)
+    plain_ms, plain = gp.bench_churn(N, R, SEED, batched=False, use_graph=False,
+                                     warmup=1, steps=max(1, args.steps // 2))
+    plain_v = (plain.mallocs_ok + plain.frees) / (plain.ms_total / 1e3)
+    latency["plain"] = lat(gp, False)
+    errors |= gp.error_word()
+    gp.close()
 
     if rank != 0:
         return
@@ -304,7 +341,9 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic (Philox4x32-10 seed 1; sizes log-uniform 16 B-4 KiB rounded to pow2)",
         "config": {"workload": WORKLOAD, "path": "batched: CTA-aggregated persistent kernels, one CUDA graph per step",
-                   "arena_bytes": ARENA, "threads_per_round": N, "rounds": R,
+                   "pinned_slots_batched": args.slots or "one per SM", "pinned_slots_plain": "128 halving to 4",
+                   "batched_knobs": {"gather_unlocked_below": args.unlocked, "segment_mib": args.segment_mib},
+                   "arena_bytes": arena, "threads_per_round": N, "rounds": R,
                    "l2": "no flush needed: 512 MiB pointer table and 16 GiB arena exceed the 129 MB L2",
                    "plain_ops_per_s": plain_v, "batched_over_plain": value / plain_v / world,
                    "mallocs_per_step": per_step_mallocs, "mallocs_failed": res.mallocs_failed,
@@ -319,6 +358,7 @@ def main():
         "e2e": {"value": e2e_v, "unit": "ops/s", "h2d_bytes_per_step": int(eres.h2d_bytes),
                 "d2h_bytes_per_step": int(eres.d2h_bytes),
                 "path": "gal_malloc_batched/gal_free_batched C ABI, sizes H2D from pinned host each round"},
+        "latency": latency,
         "gpu_launches": int(res.malloc_launches + res.free_launches),
         "clocks": clk.summary(),
     }

@@ -90,6 +90,7 @@ def lib():
         "gal_bench_churn_e2e": ([vp, vp, u64, u32, u32, C.c_int, C.c_int, vp, vp], C.c_int),
         "gal_churn_sizes": ([u64, u64, u32, vp], C.c_int),
         "gal_bench_stamp": ([vp, u64, u64, C.c_int, vp, vp], C.c_int),
+        "gal_bench_latency": ([vp, u64, u32, C.c_int, vp, vp], C.c_int),
         "gal_bench_atomic_peak": ([vp, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
@@ -248,9 +249,11 @@ class Gallatin:
         _check(lib().gal_free_batched(self._h, _ptr(ptrs), ptrs.numel(), stream), "gal_free_batched")
 
     def bench_churn(self, threads_per_round, rounds, seed, batched, use_graph, warmup, steps):
+        """batched: True/False, or a mask (1: CTA-aggregated malloc, 2: CTA-aggregated free)."""
         ms = np.zeros(max(steps, 1), dtype=np.float32)
         r = ChurnResult()
-        _check(lib().gal_bench_churn(self._h, threads_per_round, rounds, seed, int(batched),
+        mode = (3 if batched else 0) if isinstance(batched, bool) else int(batched)
+        _check(lib().gal_bench_churn(self._h, threads_per_round, rounds, seed, mode,
                                      int(use_graph), warmup, steps, ms.ctypes.data, C.byref(r)),
                "gal_bench_churn")
         return ms[:steps], r
@@ -262,6 +265,14 @@ class Gallatin:
                                          warmup, steps, ms.ctypes.data, C.byref(r)),
                "gal_bench_churn_e2e")
         return ms[:steps], r
+
+    def bench_latency(self, n, seed, batched):
+        """(malloc_cycles, free_cycles) per request of one churn round."""
+        m = np.zeros(n, dtype=np.uint32)
+        f = np.zeros(n, dtype=np.uint32)
+        _check(lib().gal_bench_latency(self._h, n, seed, int(batched), m.ctypes.data, f.ctypes.data),
+               "gal_bench_latency")
+        return m, f
 
     def bench_stamp(self, n, size, rounds=1):
         ms = np.zeros(2, dtype=np.float32)

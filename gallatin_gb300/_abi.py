@@ -43,6 +43,7 @@ class GalConfig(C.Structure):
         ("pinned_slots_min", C.c_uint32),
         ("zero_arena", C.c_uint32),
         ("spin_limit", C.c_uint32),
+        ("gather_unlocked_below", C.c_uint32),
     ]
 
 

@@ -35,8 +35,8 @@ static __device__ __noinline__ void cta_claim_class(const state *s, uint32_t tre
   uint32_t assigned = 0, nruns = 0;
   for (int attempt = 0; attempt < CTA_CLAIM_ATTEMPTS && assigned < want && nruns < CTA_RUNS;
        attempt++) {
-    uint32_t slot = pick_slot(s, tree);
-    uint32_t blk = ld_rlx(s->slots + s->slot_base[tree] + slot);
+    uint32_t blk;
+    uint32_t slot = pick_slot(s, tree, blk);
     if (blk == NOBLK) {
       backoff((uint32_t)attempt);
       continue;
@@ -44,7 +44,10 @@ static __device__ __noinline__ void cta_claim_class(const state *s, uint32_t tre
     uint32_t need = want - assigned;
     unsigned long long old = atomicAdd(&s->mwords[blk], (unsigned long long)need);
     uint64_t cnt = old & 0xFFFFFFFFull;
-    if (cnt >= SLICES_PER_BLOCK) continue;  // exhausted; its crosser is replacing it
+    if (cnt >= SLICES_PER_BLOCK) {  // exhausted; its crosser is installing a new one
+      __nanosleep(256);
+      continue;
+    }
     uint32_t got = (uint32_t)min((uint64_t)need, (uint64_t)SLICES_PER_BLOCK - cnt);
     bool crossed = cnt + need > SLICES_PER_BLOCK - 1;
     if ((uint32_t)(old >> 32) == tree) {

@@ -149,6 +149,67 @@ __global__ void k_stamp_free(const gal::state *s, uint64_t n, uint64_t **ptrs,
   galwl::warp_count(&stats[3], p != nullptr);
 }
 
+// per-request latency: clock64() around each malloc / free of one churn round
+__global__ void k_lat_malloc_plain(const gal::state *s, void **ptrs, uint64_t base, uint64_t n,
+                                   uint32_t seed, uint32_t *cycles) {
+  uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  uint64_t size = galwl::mixed_size(base + t, seed);
+  long long c0 = clock64();
+  void *p = gal::malloc(s, size);
+  long long c1 = clock64();
+  if (p) *(volatile uint32_t *)p = galwl::payload(base + t, seed);
+  ptrs[base + t] = p;
+  cycles[t] = (uint32_t)min(c1 - c0, 0xFFFFFFFFll);
+}
+
+__global__ void k_lat_free_plain(const gal::state *s, void **ptrs, uint64_t base, uint64_t n,
+                                 uint32_t *cycles) {
+  uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  void *p = ptrs[base + t];
+  long long c0 = clock64();
+  if (p) gal::free(s, p);
+  long long c1 = clock64();
+  ptrs[base + t] = nullptr;
+  cycles[t] = (uint32_t)min(c1 - c0, 0xFFFFFFFFll);
+}
+
+__global__ void __launch_bounds__(BT)
+    k_lat_malloc_batched(const gal::state *s, void **ptrs, uint64_t base, uint64_t n, uint32_t seed,
+                         uint32_t *cycles) {
+  __shared__ gal::cta_claim_smem sm;
+  for (uint64_t c = (uint64_t)blockIdx.x * BT; c < n; c += (uint64_t)gridDim.x * BT) {
+    uint64_t t = c + threadIdx.x;
+    bool has = t < n;
+    uint64_t size = has ? galwl::mixed_size(base + t, seed) : 0;
+    long long c0 = clock64();
+    void *p = gal::cta_malloc(s, size, has, sm);
+    long long c1 = clock64();
+    if (has) {
+      if (p) *(volatile uint32_t *)p = galwl::payload(base + t, seed);
+      ptrs[base + t] = p;
+      cycles[t] = (uint32_t)min(c1 - c0, 0xFFFFFFFFll);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(BT)
+    k_lat_free_batched(const gal::state *s, void **ptrs, uint64_t base, uint64_t n, uint32_t *cycles) {
+  __shared__ gal::cta_free_smem<2 * BT> sm;
+  for (uint64_t c = (uint64_t)blockIdx.x * BT; c < n; c += (uint64_t)gridDim.x * BT) {
+    uint64_t t = c + threadIdx.x;
+    void *p = t < n ? ptrs[base + t] : nullptr;
+    long long c0 = clock64();
+    gal::cta_free<2 * BT>(s, p, sm);
+    long long c1 = clock64();
+    if (t < n) {
+      ptrs[base + t] = nullptr;
+      cycles[t] = (uint32_t)min(c1 - c0, 0xFFFFFFFFll);
+    }
+  }
+}
+
 // L2 atomic probe: each thread does `iters` atomicAdd (with return) on
 // distinct words of a buffer that fits in L2 (stride keeps a warp's lanes on
 // different 32-byte sectors), or on one shared word when same_address.
@@ -197,7 +258,7 @@ void enqueue_step(churn_ctx &c, cudaStream_t st, bool capturing) {
     if (r > 0) {
       uint64_t live = drain ? nslots : c.N * r;
       mark(1, true);
-      if (c.batched) {
+      if (c.batched & 2) {
         unsigned g = (unsigned)std::min<uint64_t>((live + BT - 1) / BT, (uint64_t)c.grid_b);
         k_churn_free_batched<<<g, BT, 0, st>>>(c.d, c.ptrs, live, r, c.seed, drain ? 1 : 0, c.stats);
       } else {
@@ -209,7 +270,7 @@ void enqueue_step(churn_ctx &c, cudaStream_t st, bool capturing) {
     if (drain) break;
     uint64_t base = c.N * r;
     mark(0, true);
-    if (c.batched) {
+    if (c.batched & 1) {
       unsigned g = (unsigned)std::min<uint64_t>((c.N + BT - 1) / BT, (uint64_t)c.grid_b);
       k_churn_malloc_batched<<<g, BT, 0, st>>>(c.d, c.ptrs, base, c.N, c.seed, c.stats);
     } else {
@@ -237,7 +298,8 @@ extern "C" {
 
 /* Mixed-size churn.  One step = `rounds` x (coin frees of the live slots before
  * every round but the first, then threads_per_round mallocs), then a drain of
- * all live slots; every step serves the same requests.  batched: CTA-aggregated
+ * all live slots; every step serves the same requests.  batched: bit 0 CTA-aggregated
+ * malloc, bit 1 CTA-aggregated free (else per-thread with warp teams); CTA-aggregated
  * persistent kernels; use_graph: the step is one captured CUDA graph.
  * step_ms[i]: duration of timed step i (CUDA events on the launching stream). */
 int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, uint32_t seed,
@@ -404,6 +466,44 @@ done:
   if (d_sizes) cudaFree(d_sizes);
   if (stats) cudaFree(stats);
   if (st) cudaStreamDestroy(st);
+  return rc;
+}
+
+/* Per-request latency in SM cycles (clock64) of one churn round of n mixed
+ * requests at full concurrency: malloc_cycles[i], then free_cycles[i] when the
+ * same allocations are freed.  One unmeasured round first.  Host buffers. */
+int gal_bench_latency(gal_handle *h, uint64_t n, uint32_t seed, int batched,
+                      uint32_t *malloc_cycles, uint32_t *free_cycles) {
+  if (!h || !n || !malloc_cycles || !free_cycles) return GAL_ERR_ARGS;
+  int rc = GAL_OK;
+  void **ptrs = nullptr;
+  uint32_t *cm = nullptr, *cf = nullptr;
+  const gal::state *d = (const gal::state *)gal_device_state(h);
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lat_malloc_batched, BT, 0);
+  unsigned gb = (unsigned)std::min<uint64_t>((n + BT - 1) / BT, (uint64_t)sms * (per_sm > 0 ? per_sm : 1));
+  unsigned gp = (unsigned)((n + 255) / 256);
+  CK(cudaMalloc(&ptrs, n * sizeof(void *)));
+  CK(cudaMalloc(&cm, n * 4));
+  CK(cudaMalloc(&cf, n * 4));
+  for (int r = 0; r < 2; r++) {
+    if (batched) {
+      k_lat_malloc_batched<<<gb, BT>>>(d, ptrs, 0, n, seed + r, cm);
+      k_lat_free_batched<<<gb, BT>>>(d, ptrs, 0, n, cf);
+    } else {
+      k_lat_malloc_plain<<<gp, 256>>>(d, ptrs, 0, n, seed + r, cm);
+      k_lat_free_plain<<<gp, 256>>>(d, ptrs, 0, n, cf);
+    }
+    CK(cudaDeviceSynchronize());
+  }
+  CK(cudaMemcpy(malloc_cycles, cm, n * 4, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(free_cycles, cf, n * 4, cudaMemcpyDeviceToHost));
+done:
+  if (ptrs) cudaFree(ptrs);
+  if (cm) cudaFree(cm);
+  if (cf) cudaFree(cf);
   return rc;
 }
 

@@ -242,7 +242,15 @@ int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot
   st.policy = cfg.subtree_policy;
   st.smid_override = cfg.smid_override;
   st.spin_limit = cfg.spin_limit ? cfg.spin_limit : (1u << 16);
-  // pinned slots: first, halving per tree, floored (shared_block_storage.cuh:260-267)
+  st.gather_unlocked_below = cfg.gather_unlocked_below;
+  // pinned slots: first, halving per tree, floored (shared_block_storage.cuh:260-267);
+  // pinned_slots_first == 0 asks for one slot per SM in every size class
+  if (cfg.pinned_slots_first == 0) {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+    cfg.pinned_slots_first = cfg.pinned_slots_min = (uint32_t)(sms > 0 ? sms : 1);
+    h->cfg = cfg;
+  }
   uint64_t n = cfg.pinned_slots_first, total = 0;
   for (uint32_t t = 0; t < T; t++) {
     uint64_t c = n == 0 ? 1 : n;
@@ -384,6 +392,7 @@ int gal_config_default(gal_config *cfg) {
   cfg->pinned_slots_min = 4;
   cfg->zero_arena = 1;
   cfg->spin_limit = 1u << 16;  // x backoff capped at 4 us: ~0.27 s per wait at most
+  cfg->gather_unlocked_below = 0;
   return GAL_OK;
 }
 

@@ -58,10 +58,14 @@ typedef struct gal_config {
   uint64_t max_size;            /* default 4096 B                                  */
   int32_t  smid_override;       /* -1: pinned slot from %smid; >=0: fixed value   */
   uint32_t subtree_policy;      /* GAL_POLICY_*                                    */
-  uint32_t pinned_slots_first;  /* pinned slots of tree 0 (reference: 128)        */
+  uint32_t pinned_slots_first;  /* pinned slots of tree 0 (reference: 128);
+                                   0 = one slot per SM in every size class        */
   uint32_t pinned_slots_min;    /* floor when halving per tree (reference: 4)     */
   uint32_t zero_arena;          /* 1: memset the arena at init (reference does)   */
   uint32_t spin_limit;          /* iteration cap for every device spin-wait       */
+  uint32_t gather_unlocked_below; /* size classes with fewer blocks per segment
+                                   gather segments without the class lock
+                                   (0 = always lock, as gallatin.cuh:1538)       */
 } gal_config;
 
 /* Aggregate statistics (stands in for Gallatin::print_info, gallatin.cuh:1855). */

@@ -74,6 +74,7 @@ struct state {
   int32_t smid_override;
   uint32_t spin_limit;
   uint32_t total_slots;
+  uint32_t gather_unlocked_below;  // see gal_config
   uint32_t slot_base[GAL_MAX_TREES];
   uint32_t slot_count[GAL_MAX_TREES];
   veb_shape veb;
@@ -521,10 +522,13 @@ GAL_DEVICE_COLD uint32_t request_block(const state *s, uint32_t tree, uint64_t t
   for (;;) {
     veb_ref sub = sub_tree(s, tree);
     uint64_t seg = s->policy == GAL_POLICY_LOWEST ? veb_find_first(sub) : veb_find_random(sub, tid);
+    // classes with few blocks per segment need a segment per few requests:
+    // the class lock only serialises them (serially the lock is always free)
+    const bool unlocked = blocks_in_segment(s, tree) < s->gather_unlocked_below;
     if (seg == FAIL) {
-      if (try_lock(s, tree)) {
+      if (unlocked || try_lock(s, tree)) {
         int64_t got = gather_new_segment(s, tree);
-        unlock(s, tree);
+        if (!unlocked) unlock(s, tree);
         if (got < 0) {
           // segment tree empty: nothing a retry by this thread alone changes
           if (++gather_fails >= GATHER_RETRIES) return NOBLK;
@@ -545,9 +549,9 @@ GAL_DEVICE_COLD uint32_t request_block(const state *s, uint32_t tree, uint64_t t
     uint32_t blk = get_block(s, seg, tree, last);
     if (last) {
       veb_remove(sub, seg);
-      if (try_lock(s, tree)) {
+      if (unlocked || try_lock(s, tree)) {
         gather_new_segment(s, tree);
-        unlock(s, tree);
+        if (!unlocked) unlock(s, tree);
       }
       __threadfence();
     }
@@ -626,17 +630,22 @@ GAL_DEVICE_INLINE void free_block_slices(const state *s, uint32_t blk) {
 
 // ------------------------------------------------------------------ pinned slots
 // per_size_pinned_blocks::get_valid_block_index (shared_block_storage.cuh:119-134)
-GAL_DEVICE_INLINE uint32_t pick_slot(const state *s, uint32_t tree) {
+// Returns the slot index; `blk` receives the block read from it (one read per
+// probed slot, the last one doubling as the reference's get_my_block read).
+GAL_DEVICE_INLINE uint32_t pick_slot(const state *s, uint32_t tree, uint32_t &blk) {
   const uint32_t n = s->slot_count[tree];
   const uint32_t *slots = s->slots + s->slot_base[tree];
   uint32_t smid = s->smid_override >= 0 ? (uint32_t)s->smid_override : sm_id();
   int my = (int)(smid % n);
   int original = my;
   int counter = 0;
-  while (ld_rlx(&slots[my]) == NOBLK && my != original - 1) {
+  uint32_t v = ld_rlx(&slots[my]);
+  while (v == NOBLK && my != original - 1) {
     my = (my + 1) % (int)n;
+    v = ld_rlx(&slots[my]);
     if (++counter >= SLOT_PROBE_LIMIT) break;
   }
+  blk = v;
   return (uint32_t)my;
 }
 
@@ -687,8 +696,9 @@ GAL_DEVICE_INLINE void *malloc_slices(const state *s, uint32_t tree, uint32_t co
     const uint32_t lt = lanemask_lt();
     // every lane of a team reads the same slot words in the same instruction
     // (one broadcast transaction), so the team needs no leader branch here
-    const uint32_t slot = pick_slot(s, tree);
-    const uint32_t blk = __shfl_sync(active, ld_rlx(s->slots + s->slot_base[tree] + slot), leader);
+    uint32_t seen;
+    const uint32_t slot = pick_slot(s, tree, seen);
+    const uint32_t blk = __shfl_sync(active, seen, leader);
     // teams whose slot was empty retry; the rest carry on with mask `live`
     const uint32_t live = __ballot_sync(active, blk != NOBLK);
     if (blk == NOBLK) continue;
