@@ -64,7 +64,7 @@ def parse():
     p.add_argument("--unlocked", type=int, default=16,
                    help="batched form: classes with fewer blocks per segment gather without the lock")
     p.add_argument("--segment-mib", type=int, default=64, help="batched form: segment size")
-    p.add_argument("--free-mode", default="cta", choices=["cta", "warp"],
+    p.add_argument("--free-mode", default="warp", choices=["cta", "warp"],
                    help="batched form: frees combined per CTA (shared-memory hash) or per warp team")
     p.add_argument("--quick", action="store_true", help="headline batched steps only (profiling)")
     return p.parse_args()

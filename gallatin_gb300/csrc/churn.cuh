@@ -34,23 +34,60 @@ __device__ __forceinline__ void churn_malloc_body(Alloc *a, void **ptrs, uint64_
   warp_count(&stats[1], p == nullptr);
 }
 
+__device__ __forceinline__ void warp_add(unsigned long long *ctr, uint32_t n) {
+  unsigned mask;
+  asm volatile("activemask.b32 %0;" : "=r"(mask));
+  uint32_t total = __reduce_add_sync(mask, n);
+  int leader = __ffs(mask) - 1;
+  if ((int)(threadIdx.x & 31) == leader && total) atomicAdd(ctr, (unsigned long long)total);
+}
+
+// Each thread of the free phase owns FREE_SLOTS consecutive slots: one vector
+// load of their pointers, one Philox group of coins for all of them.
+constexpr int FREE_SLOTS = 4;
+
+__device__ __forceinline__ uint64_t free_threads(uint64_t nslots) {
+  return (nslots + FREE_SLOTS - 1) / FREE_SLOTS;
+}
+
+__device__ __forceinline__ void load_slots(void **ptrs, uint64_t i0, uint64_t nslots, void *p[FREE_SLOTS]) {
+  if (i0 + FREE_SLOTS <= nslots) {
+    ulonglong2 a = *(const ulonglong2 *)(ptrs + i0);
+    ulonglong2 b = *(const ulonglong2 *)(ptrs + i0 + 2);
+    p[0] = (void *)a.x;
+    p[1] = (void *)a.y;
+    p[2] = (void *)b.x;
+    p[3] = (void *)b.y;
+  } else {
+#pragma unroll
+    for (int k = 0; k < FREE_SLOTS; k++) p[k] = i0 + k < nslots ? ptrs[i0 + k] : nullptr;
+  }
+}
+
 // all == true frees every live slot (drain); otherwise a fair coin per slot.
 template <class Alloc>
 __device__ __forceinline__ void churn_free_body(Alloc *a, void **ptrs, uint64_t nslots,
                                                 uint32_t round, uint32_t seed, bool all,
                                                 unsigned long long *stats) {
-  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nslots) return;
-  void *p = ptrs[i];
-  bool go = p != nullptr && (all || free_coin(i, round, seed));
-  bool bad = false;
-  if (go) {
-    bad = *(volatile uint32_t *)p != payload(i, seed);
-    a->free(p);
-    ptrs[i] = nullptr;
+  uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t i0 = t * FREE_SLOTS;
+  if (i0 >= nslots) return;
+  void *p[FREE_SLOTS];
+  load_slots(ptrs, i0, nslots, p);
+  u32x4 coins = all ? u32x4{{~0u, ~0u, ~0u, ~0u}} : free_coin_group(i0 >> 7, round, seed);
+  uint32_t nbad = 0, ngo = 0;
+#pragma unroll
+  for (int k = 0; k < FREE_SLOTS; k++) {
+    uint64_t i = i0 + k;
+    if (p[k] != nullptr && coin_bit(coins, i)) {
+      nbad += *(const uint32_t *)p[k] != payload(i, seed);
+      a->free(p[k]);
+      ptrs[i] = nullptr;
+      ngo++;
+    }
   }
-  warp_count(&stats[2], bad);
-  warp_count(&stats[3], go);
+  warp_add(&stats[2], nbad);
+  warp_add(&stats[3], ngo);
 }
 
 }  // namespace galwl

@@ -110,15 +110,20 @@ struct cta_free_smem {
   uint32_t cnt[SLOTS];
 };
 
-// Frees `ptr` (nullptr = nothing); one free-counter atomic per distinct block.
-template <int SLOTS>
-__device__ __forceinline__ void cta_free(const state *s, void *ptr, cta_free_smem<SLOTS> &sm) {
+// Frees this thread's N pointers (nullptr = nothing); one free-counter atomic
+// per distinct block per CTA.  SLOTS (a power of two) must be at least
+// blockDim.x * N so the table cannot fill.
+template <int SLOTS, int N>
+__device__ __forceinline__ void cta_free(const state *s, void *const (&ptrs)[N], cta_free_smem<SLOTS> &sm) {
   for (int i = threadIdx.x; i < SLOTS; i += blockDim.x) {
     sm.key[i] = NOBLK;
     sm.cnt[i] = 0;
   }
   __syncthreads();
-  if (ptr) {
+#pragma unroll
+  for (int k = 0; k < N; k++) {
+    void *ptr = ptrs[k];
+    if (!ptr) continue;
     uint16_t tree;
     uint32_t blk = block_of(s, ptr, tree);
     bool placed = false;
@@ -140,6 +145,12 @@ __device__ __forceinline__ void cta_free(const state *s, void *ptr, cta_free_sme
   for (int i = threadIdx.x; i < SLOTS; i += blockDim.x)
     if (sm.key[i] != NOBLK) credit_frees(s, sm.key[i], sm.cnt[i]);
   __syncthreads();
+}
+
+template <int SLOTS>
+__device__ __forceinline__ void cta_free(const state *s, void *ptr, cta_free_smem<SLOTS> &sm) {
+  void *const one[1] = {ptr};
+  cta_free<SLOTS, 1>(s, one, sm);
 }
 
 }  // namespace gal

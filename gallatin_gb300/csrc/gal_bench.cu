@@ -78,21 +78,28 @@ __global__ void __launch_bounds__(BT)
 __global__ void __launch_bounds__(BT)
     k_churn_free_batched(const gal::state *s, void **ptrs, uint64_t nslots, uint32_t round,
                          uint32_t seed, int all, unsigned long long *stats) {
-  __shared__ gal::cta_free_smem<2 * BT> sm;
-  for (uint64_t c = (uint64_t)blockIdx.x * BT; c < nslots; c += (uint64_t)gridDim.x * BT) {
-    uint64_t i = c + threadIdx.x;
-    void *p = i < nslots ? ptrs[i] : nullptr;
-    bool go = p != nullptr && (all || galwl::free_coin(i, round, seed));
-    bool bad = false;
-    if (go) {
-      bad = *(volatile uint32_t *)p != galwl::payload(i, seed);
-      ptrs[i] = nullptr;
+  constexpr int F = galwl::FREE_SLOTS;
+  __shared__ gal::cta_free_smem<2 * BT * F> sm;
+  for (uint64_t c = (uint64_t)blockIdx.x * BT * F; c < nslots; c += (uint64_t)gridDim.x * BT * F) {
+    uint64_t i0 = c + (uint64_t)threadIdx.x * F;
+    void *p[F];
+    galwl::load_slots(ptrs, i0, nslots, p);
+    galwl::u32x4 coins = all ? galwl::u32x4{{~0u, ~0u, ~0u, ~0u}} : galwl::free_coin_group(i0 >> 7, round, seed);
+    uint32_t nbad = 0, ngo = 0;
+#pragma unroll
+    for (int k = 0; k < F; k++) {
+      uint64_t i = i0 + k;
+      if (p[k] != nullptr && galwl::coin_bit(coins, i)) {
+        nbad += *(const uint32_t *)p[k] != galwl::payload(i, seed);
+        ptrs[i] = nullptr;
+        ngo++;
+      } else {
+        p[k] = nullptr;
+      }
     }
-    gal::cta_free<2 * BT>(s, go ? p : nullptr, sm);
-    if (i < nslots) {
-      galwl::warp_count(&stats[2], bad);
-      galwl::warp_count(&stats[3], go);
-    }
+    gal::cta_free<2 * BT * F, F>(s, p, sm);
+    galwl::warp_add(&stats[2], nbad);
+    galwl::warp_add(&stats[3], ngo);
   }
 }
 
@@ -109,18 +116,27 @@ __global__ void k_stamp_payload(void **ptrs, uint64_t base, uint64_t n, uint32_t
 
 __global__ void k_select_frees(void **ptrs, void **freelist, uint64_t nslots, uint32_t round,
                                uint32_t seed, int all, unsigned long long *stats) {
-  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nslots) return;
-  void *p = ptrs[i];
-  bool go = p != nullptr && (all || galwl::free_coin(i, round, seed));
-  bool bad = false;
-  if (go) {
-    bad = *(volatile uint32_t *)p != galwl::payload(i, seed);
-    ptrs[i] = nullptr;
+  constexpr int F = galwl::FREE_SLOTS;
+  uint64_t i0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * F;
+  if (i0 >= nslots) return;
+  void *p[F];
+  galwl::load_slots(ptrs, i0, nslots, p);
+  galwl::u32x4 coins = all ? galwl::u32x4{{~0u, ~0u, ~0u, ~0u}} : galwl::free_coin_group(i0 >> 7, round, seed);
+  uint32_t nbad = 0, ngo = 0;
+#pragma unroll
+  for (int k = 0; k < F; k++) {
+    uint64_t i = i0 + k;
+    if (i >= nslots) break;
+    bool go = p[k] != nullptr && galwl::coin_bit(coins, i);
+    if (go) {
+      nbad += *(const uint32_t *)p[k] != galwl::payload(i, seed);
+      ptrs[i] = nullptr;
+      ngo++;
+    }
+    freelist[i] = go ? p[k] : nullptr;
   }
-  freelist[i] = go ? p : nullptr;
-  galwl::warp_count(&stats[2], bad);
-  galwl::warp_count(&stats[3], go);
+  galwl::warp_add(&stats[2], nbad);
+  galwl::warp_add(&stats[3], ngo);
 }
 
 // n threads x malloc(size) + thread-id stamp, then check + free (global_test.cu)
@@ -259,10 +275,12 @@ void enqueue_step(churn_ctx &c, cudaStream_t st, bool capturing) {
       uint64_t live = drain ? nslots : c.N * r;
       mark(1, true);
       if (c.batched & 2) {
-        unsigned g = (unsigned)std::min<uint64_t>((live + BT - 1) / BT, (uint64_t)c.grid_b);
+        const uint64_t chunk = (uint64_t)BT * galwl::FREE_SLOTS;
+        unsigned g = (unsigned)std::min<uint64_t>((live + chunk - 1) / chunk, (uint64_t)c.grid_b);
         k_churn_free_batched<<<g, BT, 0, st>>>(c.d, c.ptrs, live, r, c.seed, drain ? 1 : 0, c.stats);
       } else {
-        k_churn_free_plain<<<(unsigned)((live + 255) / 256), 256, 0, st>>>(c.d, c.ptrs, live, r, c.seed,
+        uint64_t nt = (live + galwl::FREE_SLOTS - 1) / galwl::FREE_SLOTS;
+        k_churn_free_plain<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(c.d, c.ptrs, live, r, c.seed,
                                                                           drain ? 1 : 0, c.stats);
       }
       mark(1, false);
@@ -425,7 +443,8 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
       bool drain = r == rounds;
       if (r > 0) {
         uint64_t live = drain ? nslots : N * r;
-        k_select_frees<<<(unsigned)((live + 255) / 256), 256, 0, st>>>(ptrs, freelist, live, r, seed,
+        const uint64_t nt = (live + galwl::FREE_SLOTS - 1) / galwl::FREE_SLOTS;
+        k_select_frees<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(ptrs, freelist, live, r, seed,
                                                                       drain ? 1 : 0, stats);
         int e = gal_free_batched(h, freelist, live, st);
         if (e) { rc = e; goto done; }

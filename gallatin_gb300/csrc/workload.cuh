@@ -66,11 +66,17 @@ GAL_HD uint32_t payload(uint64_t slot, uint32_t seed) {
   return (uint32_t)(slot * 0x9E3779B97F4A7C15ull >> 32) ^ seed ^ 0x5EEDu;
 }
 
-// Fair coin of slot `slot` in round `round`: decides the 50% free.
+// Fair coins of 128 consecutive slots (group = slot / 128) in round `round`:
+// one Philox call, one bit per slot.  Decides the 50% free.
+GAL_HD u32x4 free_coin_group(uint64_t group, uint32_t round, uint32_t seed) {
+  u32x4 c = {{(uint32_t)group, (uint32_t)(group >> 32), round, 0xF4EEu}};
+  return philox4x32_10(c, seed, 0xC01Du);
+}
+GAL_HD bool coin_bit(const u32x4 &g, uint64_t slot) {
+  return (g.v[(slot >> 5) & 3u] >> (slot & 31u)) & 1u;
+}
 GAL_HD bool free_coin(uint64_t slot, uint32_t round, uint32_t seed) {
-  u32x4 c = {{(uint32_t)slot, (uint32_t)(slot >> 32), round, 0xF4EEu}};
-  u32x4 r = philox4x32_10(c, seed, 0xC01Du);
-  return (r.v[2] & 1u) != 0;
+  return coin_bit(free_coin_group(slot >> 7, round, seed), slot);
 }
 
 }  // namespace galwl

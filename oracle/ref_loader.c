@@ -211,7 +211,8 @@ int ref_churn(void *h, uint64_t threads_per_round, uint32_t rounds, uint32_t see
         uint64_t live = threads_per_round * rd;
         int all = 0;
         void *fa[] = {&r->alloc, &ptrs, &live, &rd, &seed, &all, &stats};
-        int e = launch(f_cfree, (unsigned)((live + block - 1) / block), block, fa);
+        /* the free phase gives each thread 4 consecutive slots (churn.cuh) */
+        int e = launch(f_cfree, (unsigned)((live + 4 * block - 1) / (4 * block)), block, fa);
         if (e) return e;
       }
       uint64_t base = threads_per_round * rd;
@@ -223,7 +224,7 @@ int ref_churn(void *h, uint64_t threads_per_round, uint32_t rounds, uint32_t see
       int all = 1;
       uint32_t rd = rounds;
       void *fa[] = {&r->alloc, &ptrs, &nslots, &rd, &seed, &all, &stats};
-      int e = launch(f_cfree, (unsigned)((nslots + block - 1) / block), block, fa);
+      int e = launch(f_cfree, (unsigned)((nslots + 4 * block - 1) / (4 * block)), block, fa);
       if (e) return e;
     }
     CK(cuEventRecord(e1, 0));
