@@ -75,6 +75,7 @@ def lib():
         "gal_error_info": ([vp, vp], C.c_int),
         "gal_state_dims_get": ([vp, vp], C.c_int),
         "gal_export_state": ([vp, vp], C.c_int),
+        "gal_export_state_noalloc": ([vp, vp], C.c_int),
         "gal_import_state": ([vp, vp], C.c_int),
         "gal_set_smid_override": ([vp, i32], C.c_int),
         "gal_set_policy": ([vp, u32], C.c_int),
@@ -209,6 +210,14 @@ class Gallatin:
         sv = StateView(self.dims())
         v = sv.cview()
         _check(lib().gal_export_state(self._h, C.byref(v)), "gal_export_state")
+        sv.pull(v)
+        return sv
+
+    def export_noalloc(self) -> StateView:
+        """export() without any device allocation (gal_export_state_noalloc)."""
+        sv = StateView(self.dims())
+        v = sv.cview()
+        _check(lib().gal_export_state_noalloc(self._h, C.byref(v)), "gal_export_state_noalloc")
         sv.pull(v)
         return sv
 

@@ -164,6 +164,18 @@ int gal_state_dims_get(gal_handle *h, gal_state_dims *out);
 int gal_export_state(gal_handle *h, const gal_state_view *view);
 int gal_import_state(gal_handle *h, const gal_state_view *view);
 
+/* Same result as gal_export_state, without allocating device memory: for
+ * callers that cannot cudaMalloc/cudaFree at this point (a caching allocator
+ * already holds the device's memory, the snapshot must not wait for the whole
+ * device, or the device-memory budget is fixed).  No counterpart in the
+ * reference.  Stages the block counters in a fixed 1 MiB device array
+ * (GAL_NOALLOC_MAX_BLOCKS counters) that every GPU loading the library keeps
+ * until exit; larger allocators get GAL_ERR_ARGS.  The first call on a device
+ * looks the array up and should come before any stream capture; calls share
+ * the array, so calls that overlap on the GPU race. */
+#define GAL_NOALLOC_MAX_BLOCKS (1u << 18)
+int gal_export_state_noalloc(gal_handle *h, const gal_state_view *view);
+
 /* Change the pinned-slot smid override after creation (-1 = hardware). */
 int gal_set_smid_override(gal_handle *h, int32_t smid);
 /* Change the sub-tree policy after creation (GAL_POLICY_*). */
