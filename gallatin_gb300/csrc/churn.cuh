@@ -64,6 +64,18 @@ __device__ __forceinline__ void load_slots(void **ptrs, uint64_t i0, uint64_t ns
   }
 }
 
+// How an allocator frees one thread's FREE_SLOTS pointers (go[k] selects);
+// the default frees them one after another.  An allocator may specialise this
+// to overlap the work of the several frees.
+template <class Alloc>
+struct free_many {
+  static __device__ __forceinline__ void run(Alloc *a, void *const (&p)[FREE_SLOTS], const bool (&go)[FREE_SLOTS]) {
+#pragma unroll
+    for (int k = 0; k < FREE_SLOTS; k++)
+      if (go[k]) a->free(p[k]);
+  }
+};
+
 // all == true frees every live slot (drain); otherwise a fair coin per slot.
 template <class Alloc>
 __device__ __forceinline__ void churn_free_body(Alloc *a, void **ptrs, uint64_t nslots,
@@ -75,17 +87,21 @@ __device__ __forceinline__ void churn_free_body(Alloc *a, void **ptrs, uint64_t 
   void *p[FREE_SLOTS];
   load_slots(ptrs, i0, nslots, p);
   u32x4 coins = all ? u32x4{{~0u, ~0u, ~0u, ~0u}} : free_coin_group(i0 >> 7, round, seed);
+  bool go[FREE_SLOTS];
+  uint32_t seen[FREE_SLOTS];
   uint32_t nbad = 0, ngo = 0;
 #pragma unroll
-  for (int k = 0; k < FREE_SLOTS; k++) {
-    uint64_t i = i0 + k;
-    if (p[k] != nullptr && coin_bit(coins, i)) {
-      nbad += *(const uint32_t *)p[k] != payload(i, seed);
-      a->free(p[k]);
-      ptrs[i] = nullptr;
+  for (int k = 0; k < FREE_SLOTS; k++) go[k] = p[k] != nullptr && coin_bit(coins, i0 + k);
+#pragma unroll
+  for (int k = 0; k < FREE_SLOTS; k++) seen[k] = go[k] ? *(const uint32_t *)p[k] : 0u;  // loads in flight together
+#pragma unroll
+  for (int k = 0; k < FREE_SLOTS; k++)
+    if (go[k]) {
+      nbad += seen[k] != payload(i0 + k, seed);
+      ptrs[i0 + k] = nullptr;
       ngo++;
     }
-  }
+  free_many<Alloc>::run(a, p, go);
   warp_add(&stats[2], nbad);
   warp_add(&stats[3], ngo);
 }

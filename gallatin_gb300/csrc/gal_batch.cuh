@@ -21,6 +21,8 @@ static constexpr int CTA_RUNS = 4;          // block runs a class may use per cl
 static constexpr int CTA_CLAIM_ATTEMPTS = 64;
 
 struct cta_claim_smem {
+  uint32_t cached[GAL_MAX_TREES];       // block a persistent CTA last claimed from, per class
+  uint32_t cached_slot[GAL_MAX_TREES];
   uint32_t count[GAL_MAX_TREES];
   uint32_t nruns[GAL_MAX_TREES];
   uint32_t run_blk[GAL_MAX_TREES][CTA_RUNS];
@@ -33,23 +35,29 @@ static __device__ __noinline__ void cta_claim_class(const state *s, uint32_t tre
                                              cta_claim_smem &sm) {
   const uint64_t tid = thread_linear_id();
   uint32_t assigned = 0, nruns = 0;
+  // a persistent CTA keeps claiming from the block it used last and reads the
+  // pinned slot again only after a claim comes back exhausted or foreign
+  uint32_t blk = sm.cached[tree], slot = sm.cached_slot[tree];
   for (int attempt = 0; attempt < CTA_CLAIM_ATTEMPTS && assigned < want && nruns < CTA_RUNS;
        attempt++) {
-    uint32_t blk;
-    uint32_t slot = pick_slot(s, tree, blk);
     if (blk == NOBLK) {
-      backoff((uint32_t)attempt);
-      continue;
+      slot = pick_slot(s, tree, blk);
+      if (blk == NOBLK) {
+        backoff((uint32_t)attempt);
+        continue;
+      }
     }
     uint32_t need = want - assigned;
     unsigned long long old = atomicAdd(&s->mwords[blk], (unsigned long long)need);
     uint64_t cnt = old & 0xFFFFFFFFull;
     if (cnt >= SLICES_PER_BLOCK) {  // exhausted; its crosser is installing a new one
+      blk = NOBLK;
       __nanosleep(256);
       continue;
     }
     uint32_t got = (uint32_t)min((uint64_t)need, (uint64_t)SLICES_PER_BLOCK - cnt);
     bool crossed = cnt + need > SLICES_PER_BLOCK - 1;
+    uint32_t used = blk;
     if ((uint32_t)(old >> 32) == tree) {
       sm.run_blk[tree][nruns] = blk;
       sm.run_start[tree][nruns] = (uint32_t)cnt;
@@ -58,10 +66,24 @@ static __device__ __noinline__ void cta_claim_class(const state *s, uint32_t tre
       assigned += got;
     } else {
       credit_frees(s, blk, got);  // foreign block: give the slices back
+      blk = NOBLK;
     }
-    if (crossed) replace_block(s, tree, slot, blk, tid);
+    if (crossed) {
+      replace_block(s, tree, slot, used, tid);
+      blk = NOBLK;
+    }
   }
   sm.nruns[tree] = nruns;
+  sm.cached[tree] = blk;
+  sm.cached_slot[tree] = slot;
+}
+
+// Call once at the start of a kernel that uses cta_malloc, before its loop.
+__device__ __forceinline__ void cta_claim_init(cta_claim_smem &sm) {
+  if (threadIdx.x < GAL_MAX_TREES) {
+    sm.cached[threadIdx.x] = NOBLK;
+    sm.cached_slot[threadIdx.x] = 0;
+  }
 }
 
 // Returns this thread's allocation (nullptr when has_request is false).

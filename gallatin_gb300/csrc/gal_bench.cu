@@ -39,6 +39,19 @@ struct plain_alloc {
   __device__ void free(void *p) { gal::free(s, p); }
 };
 
+}  // namespace
+
+// this library frees a thread's pointers with overlapped lookups and atomics
+template <>
+struct galwl::free_many<plain_alloc> {
+  static __device__ __forceinline__ void run(plain_alloc *a, void *const (&p)[galwl::FREE_SLOTS],
+                                             const bool (&go)[galwl::FREE_SLOTS]) {
+    gal::free_n<galwl::FREE_SLOTS>(a->s, p, go);
+  }
+};
+
+namespace {
+
 constexpr int BT = 512;  // batched CTA size
 
 __global__ void k_churn_malloc_plain(const gal::state *s, void **ptrs, uint64_t base, uint64_t n,
@@ -59,6 +72,7 @@ __global__ void __launch_bounds__(BT)
     k_churn_malloc_batched(const gal::state *s, void **ptrs, uint64_t base, uint64_t n,
                            uint32_t seed, unsigned long long *stats) {
   __shared__ gal::cta_claim_smem sm;
+  gal::cta_claim_init(sm);
   for (uint64_t c = (uint64_t)blockIdx.x * BT; c < n; c += (uint64_t)gridDim.x * BT) {
     uint64_t t = c + threadIdx.x;
     bool has = t < n;
@@ -195,6 +209,7 @@ __global__ void __launch_bounds__(BT)
     k_lat_malloc_batched(const gal::state *s, void **ptrs, uint64_t base, uint64_t n, uint32_t seed,
                          uint32_t *cycles) {
   __shared__ gal::cta_claim_smem sm;
+  gal::cta_claim_init(sm);
   for (uint64_t c = (uint64_t)blockIdx.x * BT; c < n; c += (uint64_t)gridDim.x * BT) {
     uint64_t t = c + threadIdx.x;
     bool has = t < n;

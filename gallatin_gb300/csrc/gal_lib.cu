@@ -173,6 +173,7 @@ constexpr int BATCH_THREADS = 512;
 __global__ void __launch_bounds__(BATCH_THREADS)
     k_malloc_batched(const gal::state *s, const uint64_t *sizes, uint64_t n, void **out) {
   __shared__ gal::cta_claim_smem sm;
+  gal::cta_claim_init(sm);
   for (uint64_t base = (uint64_t)blockIdx.x * BATCH_THREADS; base < n;
        base += (uint64_t)gridDim.x * BATCH_THREADS) {
     uint64_t i = base + threadIdx.x;

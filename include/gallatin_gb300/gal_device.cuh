@@ -609,8 +609,12 @@ GAL_DEVICE_COLD void return_block(const state *s, uint32_t blk) {
 
 // Block::block_free_multiple + reset_free + free_block (block.cuh:87-98,200-212,
 // gallatin.cuh:1732-1766)
+GAL_DEVICE_INLINE void credit_done(const state *s, uint32_t blk, uint32_t old, uint32_t n);
 GAL_DEVICE_INLINE void credit_frees(const state *s, uint32_t blk, uint32_t n) {
-  uint32_t old = atomicAdd(&s->fctr[blk], n);
+  credit_done(s, blk, atomicAdd(&s->fctr[blk], n), n);
+}
+// the block's free counter was `old` before this thread added n
+GAL_DEVICE_INLINE void credit_done(const state *s, uint32_t blk, uint32_t old, uint32_t n) {
   if (old + n == SLICES_PER_BLOCK) {
     atomicExch(&s->fctr[blk], 0u);
     __threadfence();
@@ -838,6 +842,49 @@ GAL_DEVICE_INLINE uint32_t block_of(const state *s, const void *ptr, uint16_t &t
   if (tree >= s->num_trees) return NOBLK;
   uint64_t in_seg = off & ((1ull << s->seg_shift) - 1ull);
   return (uint32_t)(seg << s->bps_shift) + (uint32_t)(in_seg >> (s->min_shift + tree + 12));
+}
+
+// Frees the pointers p[k] with go[k] set, as N calls of free() would, but
+// with their table lookups and their free-counter atomics each issued back to
+// back so the round trips overlap.  Warp teams form per k, as in free().
+template <int N>
+GAL_DEVICE_INLINE void free_n(const state *s, void *const (&p)[N], const bool (&go)[N]) {
+  uint16_t tree[N];
+  uint64_t off[N];
+#pragma unroll
+  for (int k = 0; k < N; k++) {
+    tree[k] = FREE_TREE;
+    off[k] = go[k] ? (uint64_t)((char *)p[k] - s->memory) : 0;
+    if (go[k] && (off[k] >> s->seg_shift) < s->num_segments)
+      tree[k] = ld_rlx(&s->tree_ids[off[k] >> s->seg_shift]);
+  }
+  uint32_t blk[N], old[N], cnt[N];
+  bool lead[N];
+#pragma unroll
+  for (int k = 0; k < N; k++) {
+    lead[k] = false;
+    blk[k] = NOBLK;
+    if (!go[k]) continue;
+    if (tree[k] >= s->num_trees) {  // segment runs and bad pointers: the scalar path
+      gal::free(s, p[k]);
+      continue;
+    }
+    uint64_t in_seg = off[k] & ((1ull << s->seg_shift) - 1ull);
+    blk[k] = (uint32_t)((off[k] >> s->seg_shift) << s->bps_shift) +
+             (uint32_t)(in_seg >> (s->min_shift + tree[k] + 12));
+  }
+#pragma unroll
+  for (int k = 0; k < N; k++) {
+    if (blk[k] == NOBLK) continue;
+    const uint32_t active = active_lanes();
+    const uint32_t team = __match_any_sync(active, blk[k]);
+    lead[k] = (int)lane_id() == __ffs(team) - 1;
+    cnt[k] = (uint32_t)__popc(team);
+    if (lead[k]) old[k] = atomicAdd(&s->fctr[blk[k]], cnt[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < N; k++)
+    if (lead[k]) credit_done(s, blk[k], old[k], cnt[k]);
 }
 
 // bytes a request of `size` occupies (Gallatin::get_allocated_size, gallatin.cuh:1152-1183)
