@@ -64,9 +64,13 @@ def parse():
     p.add_argument("--unlocked", type=int, default=16,
                    help="batched form: classes with fewer blocks per segment gather without the lock")
     p.add_argument("--segment-mib", type=int, default=64, help="batched form: segment size")
+    p.add_argument("--min-size", type=int, default=16, help="batched form: smallest slice")
+    p.add_argument("--max-size", type=int, default=4096, help="batched form: largest slice")
     p.add_argument("--free-mode", default="warp", choices=["cta", "warp"],
                    help="batched form: frees combined per CTA (shared-memory hash) or per warp team")
     p.add_argument("--quick", action="store_true", help="headline batched steps only (profiling)")
+    p.add_argument("--configs", action="store_true",
+                   help="instead of the headline: BASELINE configs 1, 3 and 5, one JSON line")
     return p.parse_args()
 
 
@@ -238,9 +242,58 @@ def run_reference(args, world, rank):
     return line
 
 
+def run_configs():
+    """The other BASELINE configs, one JSON line: 1 (1,048,576 x 16 B tid stamp
+    on 2 GiB, ours and the reference build; the 4,096-op serial trace against
+    the oracle), 3 (large and block-size allocations, 64 GiB), 5 (served loop,
+    32 GiB)."""
+    import torch
+    import gallatin_gb300 as G
+    from gallatin_gb300 import serve
+    from gallatin_gb300.workloads import large_block_workload
+    from oracle.oracle import Oracle, gen_serial_trace
+    out = {"metric": METRIC, "configs": True}
+    n, rounds = 1 << 20, 5
+    g = G.Gallatin.generate_on_device(2 << 30, 42)
+    ms, st = g.bench_stamp(n, 16, rounds)
+    ops = float(st[0] + st[3])
+    c1 = {"ours_ops_per_s": ops / (float(ms.sum()) / 1e3), "ours_malloc_ms": float(ms[0]) / rounds,
+          "ours_free_ms": float(ms[1]) / rounds, "stamp_errors": int(st[2]), "failed": int(st[1])}
+    ops_trace = gen_serial_trace(7, 4096, 60, 16, 256)
+    t0 = time.time()
+    offs, smid = g.replay(ops_trace)
+    c1["serial_trace_s"] = time.time() - t0
+    c1["serial_offsets_equal_oracle"] = bool(np.array_equal(offs, Oracle(2 << 30, 42).replay(ops_trace, smid=smid)))
+    g.close()
+    try:
+        from oracle import refgpu
+        if refgpu.available():
+            ref = refgpu.RefGPU(2 << 30, 42, refgpu.BOOT_RACY)
+            rms, rst = ref.stamp(n, 16, rounds)
+            ref.close()
+            c1["ref_ops_per_s"] = float(rst[0] + rst[3]) / (float(rms.sum()) / 1e3)
+            c1["ref_stamp_errors"] = int(rst[2])
+    except Exception as e:  # reported, not fatal
+        c1["ref_error"] = str(e)
+    out["config1"] = c1
+    g = G.Gallatin.generate_on_device(64 << 30, 7)
+    c3 = large_block_workload(g)
+    g.close()
+    out["config3"] = c3
+    c5 = serve.serve(400, arena_bytes=32 << 30, slots=32)
+    out["config5"] = c5
+    torch.cuda.synchronize()
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup(args)
+    if args.configs:
+        import torch
+        torch.cuda.set_device(local)
+        run_configs()
+        return
     if args.impl == "reference":
         line = run_reference(args, world, rank)
         if line is not None:
@@ -256,7 +309,8 @@ def main():
     # the batched form runs with its tuned knobs; the plain per-thread form with
     # the reference's defaults (128 pinned slots halving to 4)
     tuned = dict(pinned_slots_first=args.slots, pinned_slots_min=args.slots if args.slots else 0,
-                 gather_unlocked_below=args.unlocked, bytes_per_segment=args.segment_mib << 20)
+                 gather_unlocked_below=args.unlocked, bytes_per_segment=args.segment_mib << 20,
+                 min_size=args.min_size, max_size=args.max_size)
     g = G.Gallatin.generate_on_device(arena, ALLOC_SEED, **tuned)
 
     # one probe step: a workload that does not fit would run the out-of-memory
@@ -343,7 +397,9 @@ def main():
         "data": "synthetic (Philox4x32-10 seed 1; sizes log-uniform 16 B-4 KiB rounded to pow2)",
         "config": {"workload": WORKLOAD, "path": "batched: CTA-aggregated persistent kernels, one CUDA graph per step",
                    "pinned_slots_batched": args.slots or "one per SM", "pinned_slots_plain": "128 halving to 4",
-                   "batched_knobs": {"gather_unlocked_below": args.unlocked, "segment_mib": args.segment_mib},
+                   "batched_knobs": {"gather_unlocked_below": args.unlocked, "segment_mib": args.segment_mib,
+                                     "min_size": args.min_size, "max_size": args.max_size,
+                                     "free_mode": args.free_mode},
                    "arena_bytes": arena, "threads_per_round": N, "rounds": R,
                    "l2": "no flush needed: 512 MiB pointer table and 16 GiB arena exceed the 129 MB L2",
                    "plain_ops_per_s": plain_v, "batched_over_plain": value / plain_v / world,

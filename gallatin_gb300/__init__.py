@@ -19,7 +19,8 @@ from ._abi import (FAIL, FREE_BIT, GAL_OK, GAL_POLICY_LOWEST, GAL_POLICY_REFEREN
                    GalStateDims, GalStateViewC, GalStats, StateView)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libgallatin_gb300.so")
+# GALLATIN_GB300_LIB points at another build of the library (same C ABI)
+LIB_PATH = os.environ.get("GALLATIN_GB300_LIB", os.path.join(HERE, "libgallatin_gb300.so"))
 
 _lib = None
 
@@ -93,6 +94,7 @@ def lib():
         "gal_bench_stamp": ([vp, u64, u64, C.c_int, vp, vp], C.c_int),
         "gal_bench_latency": ([vp, u64, u32, C.c_int, vp, vp], C.c_int),
         "gal_bench_atomic_peak": ([vp, vp], C.c_int),
+        "gal_job_launch": ([vp, u32, u64, u64, vp, vp, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -50,14 +50,17 @@ __device__ __forceinline__ uint64_t free_threads(uint64_t nslots) {
   return (nslots + FREE_SLOTS - 1) / FREE_SLOTS;
 }
 
+static_assert(FREE_SLOTS % 2 == 0 && FREE_SLOTS <= 128, "slots come in 16-byte pairs within a coin group");
+
+// i0 is a multiple of FREE_SLOTS, so whole pairs are 16-byte aligned
 __device__ __forceinline__ void load_slots(void **ptrs, uint64_t i0, uint64_t nslots, void *p[FREE_SLOTS]) {
   if (i0 + FREE_SLOTS <= nslots) {
-    ulonglong2 a = *(const ulonglong2 *)(ptrs + i0);
-    ulonglong2 b = *(const ulonglong2 *)(ptrs + i0 + 2);
-    p[0] = (void *)a.x;
-    p[1] = (void *)a.y;
-    p[2] = (void *)b.x;
-    p[3] = (void *)b.y;
+#pragma unroll
+    for (int k = 0; k < FREE_SLOTS; k += 2) {
+      ulonglong2 a = *(const ulonglong2 *)(ptrs + i0 + k);
+      p[k] = (void *)a.x;
+      p[k + 1] = (void *)a.y;
+    }
   } else {
 #pragma unroll
     for (int k = 0; k < FREE_SLOTS; k++) p[k] = i0 + k < nslots ? ptrs[i0 + k] : nullptr;

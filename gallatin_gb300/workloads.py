@@ -1,0 +1,112 @@
+"""Further workloads of the allocator beyond the headline churn (bench.py).
+
+large_block_workload: large and block-size allocations (64 GiB arena; requests
+log-uniform over 64 KiB–256 MiB, served as whole blocks up to 16 MiB and as
+2–16 contiguous 16 MiB segments beyond, interleaved with 64 B slices at 20
+per large request).  Fill to 70% of the arena, then 10 rounds of freeing a
+random 30% of the live allocations and refilling with fresh sizes.  The arena
+holds ~1,400 such requests at once, so a run issues a few thousand large
+requests.  Every live allocation is checked for overlap and alignment after
+each round; fragmentation = largest run of free segments / free segments.
+"""
+import numpy as np
+
+SEG = 16 << 20
+
+
+def occupied_bytes(sizes):
+    """Bytes each request holds (Gallatin::get_allocated_size, gallatin.cuh:1152)."""
+    s = np.maximum(np.asarray(sizes, dtype=np.int64), 16)
+    c = 1 << np.ceil(np.log2(s)).astype(np.int64)
+    big = s > SEG
+    c[big] = ((s[big] - 1) // SEG + 1) * SEG
+    return c
+
+
+def alignment(sizes):
+    s = np.asarray(sizes, dtype=np.int64)
+    a = occupied_bytes(s)
+    a[(s > 4096) & (s <= 32768)] = 4096
+    a[s > SEG] = SEG
+    return a
+
+
+def check_live(ptrs, sizes, base):
+    """No two live ranges overlap and each pointer has its tier's alignment."""
+    order = np.argsort(ptrs)
+    p, n, a = ptrs[order], occupied_bytes(sizes)[order], alignment(sizes)[order]
+    overlap = int((p[1:] < p[:-1] + n[:-1]).sum())
+    misaligned = int((((p - base) % a) != 0).sum())
+    return overlap, misaligned
+
+
+def large_block_workload(g, seed=3, fill=0.70, rounds=10, small_per_large=20, batch=256,
+                         free_frac=0.30):
+    import torch
+
+    rng = np.random.default_rng(seed)
+    arena = g.arena_bytes
+    target = fill * arena
+    live_p = np.zeros(0, dtype=np.int64)
+    live_s = np.zeros(0, dtype=np.int64)
+    stats = {"mallocs": 0, "frees": 0, "failed": 0, "large_requests": 0, "gpu_ms": 0.0,
+             "fragmentation": [], "overlaps": 0, "misaligned": 0}
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, *args):
+        ev0.record()
+        fn(*args)
+        ev1.record()
+        ev1.synchronize()
+        stats["gpu_ms"] += ev0.elapsed_time(ev1)
+
+    def allocate(n_large):
+        nonlocal live_p, live_s
+        large = (2 ** rng.uniform(16, 28, n_large)).astype(np.int64)
+        sizes = np.concatenate([large, np.full(n_large * small_per_large, 64, dtype=np.int64)])
+        rng.shuffle(sizes)
+        d_sizes = torch.from_numpy(sizes).cuda()
+        d_ptrs = torch.zeros(len(sizes), dtype=torch.int64, device="cuda")
+        timed(g.malloc_per_thread, d_sizes, d_ptrs)
+        ptrs = d_ptrs.cpu().numpy()
+        ok = ptrs != 0
+        stats["mallocs"] += int(ok.sum())
+        stats["failed"] += int((~ok).sum())
+        stats["large_requests"] += n_large
+        live_p = np.concatenate([live_p, ptrs[ok]])
+        live_s = np.concatenate([live_s, sizes[ok]])
+        return int((~ok[sizes > 64]).sum())
+
+    def fill_up():
+        while occupied_bytes(live_s).sum() < target:
+            if allocate(batch) > batch // 2:      # the arena is as full as it gets
+                break
+
+    def round_report():
+        o, m = check_live(live_p, live_s, g.arena_base)
+        stats["overlaps"] += o
+        stats["misaligned"] += m
+        st = g.stats()
+        frag = st.largest_free_run / st.free_segments if st.free_segments else 1.0
+        stats["fragmentation"].append(round(float(frag), 4))
+
+    fill_up()
+    round_report()
+    for _ in range(rounds):
+        victims = rng.random(len(live_p)) < free_frac
+        d_free = torch.from_numpy(live_p[victims]).cuda()
+        timed(g.free_per_thread, d_free)
+        stats["frees"] += int(victims.sum())
+        live_p, live_s = live_p[~victims], live_s[~victims]
+        fill_up()
+        round_report()
+    # drain
+    d_free = torch.from_numpy(live_p).cuda()
+    timed(g.free_per_thread, d_free)
+    stats["frees"] += len(live_p)
+    st = g.stats()
+    stats["multi_segment_allocs_after_drain"] = int(st.multi_segment_allocs)
+    stats["error_word"] = g.error_word()
+    stats["ops_per_s"] = (stats["mallocs"] + stats["frees"]) / (stats["gpu_ms"] / 1e3)
+    stats["live_fraction_target"] = fill
+    return stats

@@ -214,6 +214,20 @@ int gal_malloc_batched(gal_handle *h, const uint64_t *sizes, uint64_t n,
                        void **out_ptrs, void *stream);
 int gal_free_batched(gal_handle *h, void *const *ptrs, uint64_t n, void *stream);
 
+/* ---- served jobs (request loop, gallatin_gb300/serve.py) -------------------
+ * One job = one CTA launched on `stream` that allocates through the device
+ * allocator: GAL_JOB_VECTOR grows a device vector of n uint32 by capacity
+ * doubling (the reference's data_structs/single_vector.cuh:86-143 growth);
+ * GAL_JOB_QUEUE runs n enqueue/dequeue operations on queues of 32 B nodes.
+ * result (device u64[3], zeroed by the caller): checksum, mallocs+frees,
+ * failed mallocs.  lat (device u32[2*GAL_JOB_LAT_SAMPLES] or NULL): cycles of
+ * the first mallocs, then of the first frees, of the job's first thread. */
+#define GAL_JOB_VECTOR 0u
+#define GAL_JOB_QUEUE 1u
+#define GAL_JOB_LAT_SAMPLES 64
+int gal_job_launch(gal_handle *h, uint32_t kind, uint64_t job_id, uint64_t n,
+                   unsigned long long *result, uint32_t *lat, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -578,13 +578,11 @@ GAL_DEVICE_COLD void return_block(const state *s, uint32_t blk) {
   uint32_t live = pos % nb;
   atomicExch(s->queues + (seg << s->bps_shift) + live, blk);
   __threadfence();
-  for (uint32_t i = 0; atomicCAS(&s->fqfc[seg], pos, pos + 1) != pos; i++) {
-    if (i >= s->spin_limit) {
-      set_error(s, GAL_DEV_ERR_TIMEOUT);
-      break;
-    }
-    backoff(i);
-  }
+  // The reference finalises returns in position order with a CAS spin
+  // (memory_table.cuh:906-910) so a hand-out never meets an empty ring entry;
+  // get_block here waits (bounded) for an entry still in flight instead, so a
+  // return only counts itself, leaving the same counter value.
+  atomicAdd(&s->fqfc[seg], 1u);
   // re-register at the 10% crossing (gallatin.cuh:1646): live/nb >= 0.1 and
   // (live-1)/nb < 0.1 in doubles; for the power-of-two nb used here that is
   // 10*live > nb >= 10*(live-1) with live-1 taken as unsigned (live 0 never).
