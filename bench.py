@@ -161,6 +161,16 @@ def sum_over_ranks(x, world):
     return _reduce_over_ranks(x, world, "SUM")
 
 
+def measured_hbm_peak():
+    """HBM copy bandwidth (GB/s) measured on this GPU model (MEASURED_PEAKS.json),
+    else the fallback figure of one earlier GB300 measurement."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "of measured (MEASURED_PEAKS.json hbm_gbs, STREAM-style copy)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "of fallback (6.8 TB/s, one earlier GB300 copy measurement)"
+
+
 def read_profile_traffic(kernel):
     """Per-launch DRAM bytes of `kernel` at the full workload, from the committed
     ncu summary profiles/<kernel>.md (line `traffic_bytes_per_launch: N`)."""
@@ -242,46 +252,53 @@ def run_reference(args, world, rank):
     return line
 
 
-def run_configs():
-    """The other BASELINE configs, one JSON line: 1 (1,048,576 x 16 B tid stamp
-    on 2 GiB, ours and the reference build; the 4,096-op serial trace against
-    the oracle), 3 (large and block-size allocations, 64 GiB), 5 (served loop,
-    32 GiB)."""
+def run_configs(impl):
+    """The secondary workloads, one JSON line.  Ours: the 1,048,576 x 16 B tid
+    stamp on 2 GiB (the drop-in per-thread path) and the time of a 4,096-op
+    serial trace replayed by one thread; large and block-size allocations on
+    64 GiB; the served request loop on 32 GiB.  --impl reference: the same
+    stamp through the reference build."""
     import torch
+    n, rounds = 1 << 20, 20
+    out = {"metric": METRIC, "configs": True}
+    if impl == "reference":
+        from oracle import refgpu
+        out["impl"] = "reference"
+        if not refgpu.available():
+            out["unavailable"] = "reference build missing (make -C oracle _ref/libref_loader.so)"
+            print(json.dumps(out))
+            return
+        ref = refgpu.RefGPU(2 << 30, 42, refgpu.BOOT_RACY)
+        ref.stamp(n, 16, 1)  # untimed round: first segment gathers
+        rms, rst = ref.stamp(n, 16, rounds)
+        ref.close()
+        out["stamp"] = {"ops_per_s": float(rst[0] + rst[3]) / (float(rms.sum()) / 1e3),
+                        "malloc_ms": float(rms[0]) / rounds, "free_ms": float(rms[1]) / rounds,
+                        "stamp_errors": int(rst[2]), "failed": int(rst[1]), "rounds": rounds}
+        print(json.dumps(out))
+        return
     import gallatin_gb300 as G
     from gallatin_gb300 import serve
-    from gallatin_gb300.workloads import large_block_workload
-    from oracle.oracle import Oracle, gen_serial_trace
-    out = {"metric": METRIC, "configs": True}
-    n, rounds = 1 << 20, 5
+    from gallatin_gb300.workloads import large_block_workload, serial_trace
     g = G.Gallatin.generate_on_device(2 << 30, 42)
+    g.bench_stamp(n, 16, 1)  # untimed round: module load and first segment gathers
     ms, st = g.bench_stamp(n, 16, rounds)
-    ops = float(st[0] + st[3])
-    c1 = {"ours_ops_per_s": ops / (float(ms.sum()) / 1e3), "ours_malloc_ms": float(ms[0]) / rounds,
-          "ours_free_ms": float(ms[1]) / rounds, "stamp_errors": int(st[2]), "failed": int(st[1])}
-    ops_trace = gen_serial_trace(7, 4096, 60, 16, 256)
+    g.close()
+    out["stamp"] = {"ops_per_s": float(st[0] + st[3]) / (float(ms.sum()) / 1e3),
+                    "malloc_ms": float(ms[0]) / rounds, "free_ms": float(ms[1]) / rounds,
+                    "stamp_errors": int(st[2]), "failed": int(st[1]), "rounds": rounds}
+    g = G.Gallatin.generate_on_device(2 << 30, 42)
+    ops_trace = serial_trace(7, 4096)
     t0 = time.time()
-    offs, smid = g.replay(ops_trace)
-    c1["serial_trace_s"] = time.time() - t0
-    c1["serial_offsets_equal_oracle"] = bool(np.array_equal(offs, Oracle(2 << 30, 42).replay(ops_trace, smid=smid)))
+    offs, _ = g.replay(ops_trace)
+    out["serial_trace"] = {"ops": len(ops_trace), "s": time.time() - t0,
+                           "failed": int((offs[ops_trace < (1 << 63)] == G.FAIL).sum()),
+                           "error_word": g.error_word()}
     g.close()
-    try:
-        from oracle import refgpu
-        if refgpu.available():
-            ref = refgpu.RefGPU(2 << 30, 42, refgpu.BOOT_RACY)
-            rms, rst = ref.stamp(n, 16, rounds)
-            ref.close()
-            c1["ref_ops_per_s"] = float(rst[0] + rst[3]) / (float(rms.sum()) / 1e3)
-            c1["ref_stamp_errors"] = int(rst[2])
-    except Exception as e:  # reported, not fatal
-        c1["ref_error"] = str(e)
-    out["config1"] = c1
     g = G.Gallatin.generate_on_device(64 << 30, 7)
-    c3 = large_block_workload(g)
+    out["large"] = large_block_workload(g)
     g.close()
-    out["config3"] = c3
-    c5 = serve.serve(400, arena_bytes=32 << 30, slots=32)
-    out["config5"] = c5
+    out["serve"] = serve.serve(400, arena_bytes=32 << 30, slots=32)
     torch.cuda.synchronize()
     print(json.dumps(out))
 
@@ -292,7 +309,7 @@ def main():
     if args.configs:
         import torch
         torch.cuda.set_device(local)
-        run_configs()
+        run_configs(args.impl)
         return
     if args.impl == "reference":
         line = run_reference(args, world, rank)
@@ -363,18 +380,28 @@ def main():
                 "free_p99_cycles": float(np.percentile(fc, 99))}
     latency = {"requests": N, "batched": lat(g, True)}
 
-    # roofline: the dominant kernel (malloc or free phase), 1 algorithmic atomic per op
+    # roofline of the dominant kernel (malloc or free phase).  HBM: algorithmic
+    # bytes per launch -- malloc: 8 B pointer store + 4 B payload store per
+    # request; free: 8 B pointer load per slot scanned (rounds 1..R-1 scan
+    # r*N slots, the drain R*N) + 4 B payload load + 8 B pointer clear per
+    # free; allocator metadata stays in L2.  L2 atomics: one counter atomic
+    # per request (the per-block malloc or free counter) against the measured
+    # atomic peak.
     distinct, same = G.atomic_peak()
     per_step_mallocs = res.mallocs_ok / args.steps
     if res.ms_malloc_kernels >= res.ms_free_kernels:
         kern, ms_k, n_launch, units = ("k_churn_malloc_batched", res.ms_malloc_kernels,
                                        res.malloc_launches, res.mallocs_ok)
+        alg_bytes = 12.0 * res.mallocs_ok
     else:
         kern, ms_k, n_launch, units = (
             "k_churn_free_batched" if args.free_mode == "cta" else "k_churn_free_plain",
             res.ms_free_kernels, res.free_launches, res.frees)
+        alg_bytes = 8.0 * N * R * (R + 1) / 2 * args.steps + 12.0 * res.frees
     avg_launch_s = ms_k / 1e3 / n_launch
     achieved = (units / n_launch) / avg_launch_s
+    hbm_achieved = (alg_bytes / n_launch) / avg_launch_s
+    hbm_peak, peak_src = measured_hbm_peak()
     traffic = read_profile_traffic(kern)
     errors = g.error_word()
     g.close()
@@ -406,12 +433,16 @@ def main():
                    "mallocs_per_step": per_step_mallocs, "mallocs_failed": res.mallocs_failed,
                    "payload_mismatch": res.payload_mismatch, "device_error_word": errors,
                    "wall_s_timed": wall},
-        "roofline": {"bound": "l2_atomic", "kernel": kern, "achieved": achieved / 1e9,
-                     "peak": distinct / 1e9, "unit": "Gatomic/s", "frac": achieved / distinct,
-                     "traffic": traffic, "atomics_per_unit": 1,
-                     "peak_source": "measured in this run: atomicAdd.u32 with return, distinct "
-                                    "addresses in a 32 MiB L2-resident buffer",
-                     "same_address_peak": same / 1e9},
+        "roofline": {"bound": "hbm", "kernel": kern, "achieved": hbm_achieved / 1e9,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": hbm_achieved / 1e9 / hbm_peak,
+                     "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes / n_launch,
+                     "peak_source": peak_src,
+                     "l2_atomic": {"achieved": achieved / 1e9, "peak": distinct / 1e9,
+                                   "unit": "Gatomic/s", "frac": achieved / distinct,
+                                   "atomics_per_unit": 1,
+                                   "peak_source": "measured in this run: atomicAdd.u32 with return, "
+                                                  "distinct addresses in a 32 MiB L2-resident buffer",
+                                   "same_address_peak": same / 1e9}},
         "e2e": {"value": e2e_v, "unit": "ops/s", "h2d_bytes_per_step": int(eres.h2d_bytes),
                 "d2h_bytes_per_step": int(eres.d2h_bytes),
                 "path": "gal_malloc_batched/gal_free_batched C ABI, sizes H2D from pinned host each round"},

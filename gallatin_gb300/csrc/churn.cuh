@@ -20,16 +20,33 @@ __device__ __forceinline__ void warp_count(unsigned long long *ctr, bool flag) {
   if ((int)(threadIdx.x & 31) == leader && b) atomicAdd(ctr, (unsigned long long)__popc(b));
 }
 
+// Slot liveness: bit (i & 31) of live_bits[i >> 5] is set while slot i holds
+// a live allocation.  A round's mallocs write the words of their slots, one
+// word per warp of 32 consecutive slots; a free phase reads the words (8 MiB
+// for 64 Mi slots, so they stay in L2), loads pointer and payload of the
+// slots it frees only, and clears their bits.  Slots freed in earlier rounds
+// are thus never read again.  Rounds are a multiple of SLOT_ALIGN requests,
+// so every warp covers whole words (and whole coin groups) or none.
+constexpr uint64_t SLOT_ALIGN = 128;
+
+// one full warp, lane l holding slot (slot & ~31) + l
+__device__ __forceinline__ void publish_live(uint32_t *live_bits, uint64_t slot, bool live) {
+  const uint32_t b = __ballot_sync(0xFFFFFFFFu, live);
+  if ((threadIdx.x & 31) == 0) live_bits[slot >> 5] = b;
+}
+
 template <class Alloc>
-__device__ __forceinline__ void churn_malloc_body(Alloc *a, void **ptrs, uint64_t base, uint64_t n,
-                                                  uint32_t seed, unsigned long long *stats) {
+__device__ __forceinline__ void churn_malloc_body(Alloc *a, void **ptrs, uint32_t *live_bits,
+                                                  uint64_t base, uint64_t n, uint32_t seed,
+                                                  unsigned long long *stats) {
   uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid >= n) return;
+  if (tid >= n) return;  // whole warps: n is a multiple of SLOT_ALIGN
   uint64_t slot = base + tid;
   uint64_t size = mixed_size(slot, seed);
   void *p = a->malloc(size);
   if (p) *(volatile uint32_t *)p = payload(slot, seed);
   ptrs[slot] = p;
+  publish_live(live_bits, slot, p != nullptr);
   warp_count(&stats[0], p != nullptr);
   warp_count(&stats[1], p == nullptr);
 }
@@ -45,10 +62,6 @@ __device__ __forceinline__ void warp_add(unsigned long long *ctr, uint32_t n) {
 // Each thread of the free phase owns FREE_SLOTS consecutive slots: one vector
 // load of their pointers, one Philox group of coins for all of them.
 constexpr int FREE_SLOTS = 4;
-
-__device__ __forceinline__ uint64_t free_threads(uint64_t nslots) {
-  return (nslots + FREE_SLOTS - 1) / FREE_SLOTS;
-}
 
 static_assert(FREE_SLOTS % 2 == 0 && FREE_SLOTS <= 128, "slots come in 16-byte pairs within a coin group");
 
@@ -79,32 +92,97 @@ struct free_many {
   }
 };
 
+constexpr uint32_t GROUP_MASK = (1u << FREE_SLOTS) - 1u;
+constexpr int GROUPS_PER_WORD = 32 / FREE_SLOTS;
+static_assert(32 % FREE_SLOTS == 0, "a thread's slots sit inside one liveness word");
+
+// The slots of i0..i0+FREE_SLOTS-1 to free: live ones, and of those the ones
+// whose coin (one Philox call per 128 slots) came up, or all on the drain.
+__device__ __forceinline__ uint32_t select_frees(uint32_t word, uint64_t i0, uint32_t round,
+                                                 uint32_t seed, bool all) {
+  uint32_t sel = (word >> (i0 & 31)) & GROUP_MASK;
+  if (sel && !all) {
+    u32x4 coins = free_coin_group(i0 >> 7, round, seed);
+    sel &= (coins.v[(i0 >> 5) & 3u] >> (i0 & 31)) & GROUP_MASK;
+  }
+  return sel;
+}
+
+// Clears the freed bits: the GROUPS_PER_WORD lanes sharing a word OR their
+// masks together and the first of them stores the word.  Full warp.
+__device__ __forceinline__ void clear_live(uint32_t *live_bits, uint64_t i0, uint32_t word,
+                                           uint32_t sel) {
+  uint32_t cleared = sel << (i0 & 31);
+#pragma unroll
+  for (int o = 1; o < GROUPS_PER_WORD; o <<= 1) cleared |= __shfl_xor_sync(0xFFFFFFFFu, cleared, o);
+  if ((threadIdx.x & (GROUPS_PER_WORD - 1)) == 0 && cleared) live_bits[i0 >> 5] = word & ~cleared;
+}
+
+// The free phase, persistent: each warp takes 1,024 slots (32 liveness words)
+// at a time.  Lane l reads word l, draws its coins (one Philox call gives the
+// coins of 128 slots, so word w uses lane w & 3 of group w >> 2) and clears the
+// bits it frees; the selected slots go, in slot order, to the warp's list in
+// shared memory, and the lanes then free them FREE_SLOTS at a time, lane l
+// taking entries l, l + 32, ... so that neighbouring lanes hold neighbouring
+// slots (which share blocks).  Dead and unselected slots cost one bit of an
+// L2-resident word; every lane has a request to serve while any is left.
 // all == true frees every live slot (drain); otherwise a fair coin per slot.
+constexpr int WARP_WORDS = 32;
+constexpr int WARP_SLOTS = 32 * WARP_WORDS;
+
 template <class Alloc>
-__device__ __forceinline__ void churn_free_body(Alloc *a, void **ptrs, uint64_t nslots,
-                                                uint32_t round, uint32_t seed, bool all,
-                                                unsigned long long *stats) {
-  uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  uint64_t i0 = t * FREE_SLOTS;
-  if (i0 >= nslots) return;
-  void *p[FREE_SLOTS];
-  load_slots(ptrs, i0, nslots, p);
-  u32x4 coins = all ? u32x4{{~0u, ~0u, ~0u, ~0u}} : free_coin_group(i0 >> 7, round, seed);
-  bool go[FREE_SLOTS];
-  uint32_t seen[FREE_SLOTS];
+__device__ __forceinline__ void churn_free_warps(Alloc *a, void **ptrs, uint32_t *live_bits,
+                                                 uint64_t nslots, uint32_t round, uint32_t seed,
+                                                 bool all, unsigned long long *stats,
+                                                 uint16_t *list /* WARP_SLOTS entries */) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint64_t words = nslots >> 5;
   uint32_t nbad = 0, ngo = 0;
+  for (uint64_t w0 = warp * WARP_WORDS; w0 < words; w0 += nwarps * WARP_WORDS) {
+    const uint64_t w = w0 + lane;
+    const uint32_t word = w < words ? live_bits[w] : 0u;
+    uint32_t sel = word;
+    if (sel && !all) sel &= free_coin_group(w >> 2, round, seed).v[w & 3u];
+    if (sel) live_bits[w] = word & ~sel;
+    const uint32_t n = (uint32_t)__popc(sel);
+    uint32_t end = n;  // inclusive scan of the counts
 #pragma unroll
-  for (int k = 0; k < FREE_SLOTS; k++) go[k] = p[k] != nullptr && coin_bit(coins, i0 + k);
-#pragma unroll
-  for (int k = 0; k < FREE_SLOTS; k++) seen[k] = go[k] ? *(const uint32_t *)p[k] : 0u;  // loads in flight together
-#pragma unroll
-  for (int k = 0; k < FREE_SLOTS; k++)
-    if (go[k]) {
-      nbad += seen[k] != payload(i0 + k, seed);
-      ptrs[i0 + k] = nullptr;
-      ngo++;
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t v = __shfl_up_sync(0xFFFFFFFFu, end, o);
+      if ((int)lane >= o) end += v;
     }
-  free_many<Alloc>::run(a, p, go);
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, end, 31);
+    uint32_t pos = end - n;
+    for (uint32_t b = sel; b; b &= b - 1u) list[pos++] = (uint16_t)(lane * 32u + (uint32_t)__ffs(b) - 1u);
+    __syncwarp();
+    for (uint32_t j0 = 0; j0 < total; j0 += 32u * FREE_SLOTS) {
+      void *p[FREE_SLOTS];
+      bool go[FREE_SLOTS];
+      uint64_t slot[FREE_SLOTS];
+      uint32_t seen[FREE_SLOTS];
+#pragma unroll
+      for (int k = 0; k < FREE_SLOTS; k++) {
+        const uint32_t j = j0 + (uint32_t)k * 32u + lane;
+        slot[k] = j < total ? w0 * 32u + list[j] : 0;
+        p[k] = j < total ? ptrs[slot[k]] : nullptr;
+      }
+#pragma unroll
+      for (int k = 0; k < FREE_SLOTS; k++) {
+        go[k] = p[k] != nullptr;
+        seen[k] = go[k] ? *(const uint32_t *)p[k] : 0u;  // loads in flight together
+      }
+#pragma unroll
+      for (int k = 0; k < FREE_SLOTS; k++)
+        if (go[k]) {
+          nbad += seen[k] != payload(slot[k], seed);
+          ngo++;
+        }
+      free_many<Alloc>::run(a, p, go);
+    }
+    __syncwarp();
+  }
   warp_add(&stats[2], nbad);
   warp_add(&stats[3], ngo);
 }

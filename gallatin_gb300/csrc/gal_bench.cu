@@ -54,23 +54,26 @@ namespace {
 
 constexpr int BT = 512;  // batched CTA size
 
-__global__ void k_churn_malloc_plain(const gal::state *s, void **ptrs, uint64_t base, uint64_t n,
-                                     uint32_t seed, unsigned long long *stats) {
+__global__ void k_churn_malloc_plain(const gal::state *s, void **ptrs, uint32_t *live, uint64_t base,
+                                     uint64_t n, uint32_t seed, unsigned long long *stats) {
   plain_alloc a{s};
-  galwl::churn_malloc_body(&a, ptrs, base, n, seed, stats);
+  galwl::churn_malloc_body(&a, ptrs, live, base, n, seed, stats);
 }
 
-__global__ void k_churn_free_plain(const gal::state *s, void **ptrs, uint64_t nslots,
-                                   uint32_t round, uint32_t seed, int all,
-                                   unsigned long long *stats) {
+constexpr int FREE_BT = 256;  // free phase CTA size (persistent grid)
+
+__global__ void __launch_bounds__(FREE_BT)
+    k_churn_free_plain(const gal::state *s, void **ptrs, uint32_t *live, uint64_t nslots,
+                       uint32_t round, uint32_t seed, int all, unsigned long long *stats) {
+  __shared__ uint16_t lists[FREE_BT / 32][galwl::WARP_SLOTS];
   plain_alloc a{s};
-  galwl::churn_free_body(&a, ptrs, nslots, round, seed, all != 0, stats);
+  galwl::churn_free_warps(&a, ptrs, live, nslots, round, seed, all != 0, stats, lists[threadIdx.x >> 5]);
 }
 
 // persistent, CTA-aggregated malloc phase of one round
 __global__ void __launch_bounds__(BT)
-    k_churn_malloc_batched(const gal::state *s, void **ptrs, uint64_t base, uint64_t n,
-                           uint32_t seed, unsigned long long *stats) {
+    k_churn_malloc_batched(const gal::state *s, void **ptrs, uint32_t *live, uint64_t base,
+                           uint64_t n, uint32_t seed, unsigned long long *stats) {
   __shared__ gal::cta_claim_smem sm;
   gal::cta_claim_init(sm);
   for (uint64_t c = (uint64_t)blockIdx.x * BT; c < n; c += (uint64_t)gridDim.x * BT) {
@@ -79,9 +82,10 @@ __global__ void __launch_bounds__(BT)
     uint64_t slot = base + t;
     uint64_t size = has ? galwl::mixed_size(slot, seed) : 0;
     void *p = gal::cta_malloc(s, size, has, sm);
-    if (has) {
+    if (has) {  // whole warps: n is a multiple of SLOT_ALIGN
       if (p) *(volatile uint32_t *)p = galwl::payload(slot, seed);
       ptrs[slot] = p;
+      galwl::publish_live(live, slot, p != nullptr);
       galwl::warp_count(&stats[0], p != nullptr);
       galwl::warp_count(&stats[1], p == nullptr);
     }
@@ -90,65 +94,81 @@ __global__ void __launch_bounds__(BT)
 
 // persistent, CTA-aggregated free phase (coin flips, or everything when all)
 __global__ void __launch_bounds__(BT)
-    k_churn_free_batched(const gal::state *s, void **ptrs, uint64_t nslots, uint32_t round,
-                         uint32_t seed, int all, unsigned long long *stats) {
+    k_churn_free_batched(const gal::state *s, void **ptrs, uint32_t *live, uint64_t nslots,
+                         uint32_t round, uint32_t seed, int all, unsigned long long *stats) {
   constexpr int F = galwl::FREE_SLOTS;
   __shared__ gal::cta_free_smem<2 * BT * F> sm;
   for (uint64_t c = (uint64_t)blockIdx.x * BT * F; c < nslots; c += (uint64_t)gridDim.x * BT * F) {
     uint64_t i0 = c + (uint64_t)threadIdx.x * F;
+    const bool valid = i0 < nslots;  // whole warps: nslots is a multiple of SLOT_ALIGN
+    const uint32_t word = valid ? live[i0 >> 5] : 0u;
+    const uint32_t sel = galwl::select_frees(word, i0, round, seed, all != 0);
     void *p[F];
-    galwl::load_slots(ptrs, i0, nslots, p);
-    galwl::u32x4 coins = all ? galwl::u32x4{{~0u, ~0u, ~0u, ~0u}} : galwl::free_coin_group(i0 >> 7, round, seed);
+    if (sel) {
+      galwl::load_slots(ptrs, i0, nslots, p);
+    } else {
+#pragma unroll
+      for (int k = 0; k < F; k++) p[k] = nullptr;
+    }
     uint32_t nbad = 0, ngo = 0;
 #pragma unroll
     for (int k = 0; k < F; k++) {
-      uint64_t i = i0 + k;
-      if (p[k] != nullptr && galwl::coin_bit(coins, i)) {
-        nbad += *(const uint32_t *)p[k] != galwl::payload(i, seed);
-        ptrs[i] = nullptr;
+      if (((sel >> k) & 1u) && p[k] != nullptr) {
+        nbad += *(const uint32_t *)p[k] != galwl::payload(i0 + k, seed);
         ngo++;
       } else {
         p[k] = nullptr;
       }
     }
     gal::cta_free<2 * BT * F, F>(s, p, sm);
+    if (valid) galwl::clear_live(live, i0, word, sel);
     galwl::warp_add(&stats[2], nbad);
     galwl::warp_add(&stats[3], ngo);
   }
 }
 
 // end-to-end helpers: user-side kernels around the public batched entry points
-__global__ void k_stamp_payload(void **ptrs, uint64_t base, uint64_t n, uint32_t seed,
+__global__ void k_stamp_payload(void **ptrs, uint32_t *live, uint64_t base, uint64_t n, uint32_t seed,
                                 unsigned long long *stats) {
   uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
+  if (t >= n) return;  // whole warps: n is a multiple of SLOT_ALIGN
   void *p = ptrs[base + t];
   if (p) *(volatile uint32_t *)p = galwl::payload(base + t, seed);
+  galwl::publish_live(live, base + t, p != nullptr);
   galwl::warp_count(&stats[0], p != nullptr);
   galwl::warp_count(&stats[1], p == nullptr);
 }
 
-__global__ void k_select_frees(void **ptrs, void **freelist, uint64_t nslots, uint32_t round,
-                               uint32_t seed, int all, unsigned long long *stats) {
+// freelist[i] = the pointer of slot i when it is freed this round, else null
+__global__ void k_select_frees(void **ptrs, uint32_t *live, void **freelist, uint64_t nslots,
+                               uint32_t round, uint32_t seed, int all, unsigned long long *stats) {
   constexpr int F = galwl::FREE_SLOTS;
   uint64_t i0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * F;
-  if (i0 >= nslots) return;
+  if (i0 >= nslots) return;  // whole warps: nslots is a multiple of SLOT_ALIGN
+  const uint32_t word = live[i0 >> 5];
+  const uint32_t sel = galwl::select_frees(word, i0, round, seed, all != 0);
   void *p[F];
-  galwl::load_slots(ptrs, i0, nslots, p);
-  galwl::u32x4 coins = all ? galwl::u32x4{{~0u, ~0u, ~0u, ~0u}} : galwl::free_coin_group(i0 >> 7, round, seed);
+  if (sel) {
+    galwl::load_slots(ptrs, i0, nslots, p);
+  } else {
+#pragma unroll
+    for (int k = 0; k < F; k++) p[k] = nullptr;
+  }
   uint32_t nbad = 0, ngo = 0;
 #pragma unroll
   for (int k = 0; k < F; k++) {
-    uint64_t i = i0 + k;
-    if (i >= nslots) break;
-    bool go = p[k] != nullptr && galwl::coin_bit(coins, i);
+    bool go = ((sel >> k) & 1u) && p[k] != nullptr;
     if (go) {
-      nbad += *(const uint32_t *)p[k] != galwl::payload(i, seed);
-      ptrs[i] = nullptr;
+      nbad += *(const uint32_t *)p[k] != galwl::payload(i0 + k, seed);
       ngo++;
+    } else {
+      p[k] = nullptr;
     }
-    freelist[i] = go ? p[k] : nullptr;
   }
+#pragma unroll
+  for (int k = 0; k < F; k += 2)
+    *(ulonglong2 *)(freelist + i0 + k) = make_ulonglong2((unsigned long long)p[k], (unsigned long long)p[k + 1]);
+  galwl::clear_live(live, i0, word, sel);
   galwl::warp_add(&stats[2], nbad);
   galwl::warp_add(&stats[3], ngo);
 }
@@ -263,8 +283,10 @@ struct churn_ctx {
   uint32_t R, seed;
   int batched;
   void **ptrs;
+  uint32_t *live;  // slot liveness bits (churn.cuh)
   unsigned long long *stats;
-  int grid_b;
+  int grid_b;  // persistent grids: batched malloc/free, warp free phase
+  int grid_f;
   std::vector<cudaEvent_t> ev;  // [2 per kernel]
   int nk = 0;
   std::vector<int> kind;        // 0 malloc, 1 free
@@ -287,16 +309,18 @@ void enqueue_step(churn_ctx &c, cudaStream_t st, bool capturing) {
   for (uint32_t r = 0; r <= c.R; r++) {
     bool drain = r == c.R;
     if (r > 0) {
-      uint64_t live = drain ? nslots : c.N * r;
+      uint64_t nscan = drain ? nslots : c.N * r;
       mark(1, true);
       if (c.batched & 2) {
         const uint64_t chunk = (uint64_t)BT * galwl::FREE_SLOTS;
-        unsigned g = (unsigned)std::min<uint64_t>((live + chunk - 1) / chunk, (uint64_t)c.grid_b);
-        k_churn_free_batched<<<g, BT, 0, st>>>(c.d, c.ptrs, live, r, c.seed, drain ? 1 : 0, c.stats);
+        unsigned g = (unsigned)std::min<uint64_t>((nscan + chunk - 1) / chunk, (uint64_t)c.grid_b);
+        k_churn_free_batched<<<g, BT, 0, st>>>(c.d, c.ptrs, c.live, nscan, r, c.seed, drain ? 1 : 0,
+                                               c.stats);
       } else {
-        uint64_t nt = (live + galwl::FREE_SLOTS - 1) / galwl::FREE_SLOTS;
-        k_churn_free_plain<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(c.d, c.ptrs, live, r, c.seed,
-                                                                          drain ? 1 : 0, c.stats);
+        const uint64_t chunk = (uint64_t)(FREE_BT / 32) * galwl::WARP_SLOTS;
+        unsigned g = (unsigned)std::min<uint64_t>((nscan + chunk - 1) / chunk, (uint64_t)c.grid_f);
+        k_churn_free_plain<<<g, FREE_BT, 0, st>>>(c.d, c.ptrs, c.live, nscan, r, c.seed, drain ? 1 : 0,
+                                                 c.stats);
       }
       mark(1, false);
     }
@@ -305,9 +329,9 @@ void enqueue_step(churn_ctx &c, cudaStream_t st, bool capturing) {
     mark(0, true);
     if (c.batched & 1) {
       unsigned g = (unsigned)std::min<uint64_t>((c.N + BT - 1) / BT, (uint64_t)c.grid_b);
-      k_churn_malloc_batched<<<g, BT, 0, st>>>(c.d, c.ptrs, base, c.N, c.seed, c.stats);
+      k_churn_malloc_batched<<<g, BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats);
     } else {
-      k_churn_malloc_plain<<<(unsigned)((c.N + 255) / 256), 256, 0, st>>>(c.d, c.ptrs, base, c.N, c.seed,
+      k_churn_malloc_plain<<<(unsigned)((c.N + 255) / 256), 256, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed,
                                                                         c.stats);
     }
     mark(0, false);
@@ -339,6 +363,7 @@ int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, 
                     int batched, int use_graph, int warmup, int steps, float *step_ms,
                     gal_churn_result *res) {
   if (!h || !res || !threads_per_round || !rounds || steps < 0 || warmup < 0) return GAL_ERR_ARGS;
+  if (threads_per_round % galwl::SLOT_ALIGN) return GAL_ERR_ARGS;
   int rc = GAL_OK;
   churn_ctx c;
   c.h = h;
@@ -348,6 +373,7 @@ int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, 
   c.seed = seed;
   c.batched = batched;
   c.ptrs = nullptr;
+  c.live = nullptr;
   c.stats = nullptr;
   int dev = 0, sms = 0, per_sm = 0;
   cudaStream_t st = nullptr;
@@ -360,6 +386,9 @@ int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, 
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_churn_malloc_batched, BT, 0);
   c.grid_b = sms * (per_sm > 0 ? per_sm : 1);
+  per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_churn_free_plain, FREE_BT, 0);
+  c.grid_f = sms * (per_sm > 0 ? per_sm : 1);
   c.ev.resize(2 * nkern);
   c.kind.resize(nkern);
   CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
@@ -368,6 +397,8 @@ int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, 
   CK(cudaEventCreate(&e1));
   CK(cudaMalloc(&c.ptrs, threads_per_round * rounds * sizeof(void *)));
   CK(cudaMemsetAsync(c.ptrs, 0, threads_per_round * rounds * sizeof(void *), st));
+  CK(cudaMalloc(&c.live, threads_per_round * rounds / 8));
+  CK(cudaMemsetAsync(c.live, 0, threads_per_round * rounds / 8, st));
   CK(cudaMalloc(&c.stats, 4 * sizeof(unsigned long long)));
   if (use_graph) {
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -419,6 +450,7 @@ done:
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
   if (c.ptrs) cudaFree(c.ptrs);
+  if (c.live) cudaFree(c.live);
   if (c.stats) cudaFree(c.stats);
   if (st) cudaStreamDestroy(st);
   return rc;
@@ -433,9 +465,11 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
                         uint32_t rounds, uint32_t seed, int warmup, int steps, float *step_ms,
                         gal_churn_result *res) {
   if (!h || !res || !host_sizes || !threads_per_round || !rounds) return GAL_ERR_ARGS;
+  if (threads_per_round % galwl::SLOT_ALIGN) return GAL_ERR_ARGS;
   int rc = GAL_OK;
   const uint64_t N = threads_per_round, nslots = N * rounds;
   void **ptrs = nullptr, **freelist = nullptr;
+  uint32_t *live = nullptr;
   uint64_t *d_sizes = nullptr;
   unsigned long long *stats = nullptr;
   unsigned long long hst[4];
@@ -450,6 +484,8 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
   CK(cudaMalloc(&d_sizes, N * sizeof(uint64_t)));
   CK(cudaMalloc(&stats, 4 * sizeof(unsigned long long)));
   CK(cudaMemsetAsync(ptrs, 0, nslots * sizeof(void *), st));
+  CK(cudaMalloc(&live, nslots / 8));
+  CK(cudaMemsetAsync(live, 0, nslots / 8, st));
   for (int s = 0; s < warmup + steps; s++) {
     CK(cudaStreamSynchronize(st));
     CK(cudaEventRecord(e0, st));
@@ -457,11 +493,11 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
     for (uint32_t r = 0; r <= rounds; r++) {
       bool drain = r == rounds;
       if (r > 0) {
-        uint64_t live = drain ? nslots : N * r;
-        const uint64_t nt = (live + galwl::FREE_SLOTS - 1) / galwl::FREE_SLOTS;
-        k_select_frees<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(ptrs, freelist, live, r, seed,
+        uint64_t nscan = drain ? nslots : N * r;
+        const uint64_t nt = (nscan + galwl::FREE_SLOTS - 1) / galwl::FREE_SLOTS;
+        k_select_frees<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(ptrs, live, freelist, nscan, r, seed,
                                                                       drain ? 1 : 0, stats);
-        int e = gal_free_batched(h, freelist, live, st);
+        int e = gal_free_batched(h, freelist, nscan, st);
         if (e) { rc = e; goto done; }
       }
       if (drain) break;
@@ -469,7 +505,8 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
                          cudaMemcpyHostToDevice, st));
       int e = gal_malloc_batched(h, d_sizes, N, ptrs + (uint64_t)r * N, st);
       if (e) { rc = e; goto done; }
-      k_stamp_payload<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(ptrs, (uint64_t)r * N, N, seed, stats);
+      k_stamp_payload<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(ptrs, live, (uint64_t)r * N, N, seed,
+                                                                   stats);
     }
     CK(cudaMemcpyAsync(hst, stats, sizeof(hst), cudaMemcpyDeviceToHost, st));
     CK(cudaEventRecord(e1, st));
@@ -496,6 +533,7 @@ done:
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
   if (ptrs) cudaFree(ptrs);
+  if (live) cudaFree(live);
   if (freelist) cudaFree(freelist);
   if (d_sizes) cudaFree(d_sizes);
   if (stats) cudaFree(stats);

@@ -14,6 +14,22 @@ import numpy as np
 SEG = 16 << 20
 
 
+def serial_trace(seed, nops, malloc_pct=60, quantum=16, steps=256):
+    """A one-thread trace in gal_replay_trace's encoding: malloc_pct% mallocs of
+    quantum x [1, steps] bytes, the rest free a random live earlier malloc."""
+    rng = np.random.default_rng(seed)
+    ops = np.zeros(nops, dtype=np.uint64)
+    live = []
+    for i in range(nops):
+        if not live or rng.integers(100) < malloc_pct:
+            ops[i] = quantum * (1 + int(rng.integers(steps)))
+            live.append(i)
+        else:
+            j = live.pop(int(rng.integers(len(live))))
+            ops[i] = (1 << 63) | j
+    return ops
+
+
 def occupied_bytes(sizes):
     """Bytes each request holds (Gallatin::get_allocated_size, gallatin.cuh:1152)."""
     s = np.maximum(np.asarray(sizes, dtype=np.int64), 16)

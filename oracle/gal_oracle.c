@@ -654,7 +654,13 @@ static uint64_t malloc_slice(orc_alloc *a, int tree, uint32_t alloc_count, uint3
     int end_valid = allocation + alloc_count <= 4096;
     uint32_t leftover = (uint32_t)((start_valid && end_valid) * (uint64_t)(alloc_count - 1) +
                                    (start_valid && !end_valid) * (4096 - allocation));
-    if (leftover > 0) a->fc[blk] += leftover; /* block_correct_frees */
+    if (leftover > 0) { /* block_correct_frees */
+      a->fc[blk] += leftover;
+      if ((a->fix & ORC_FIX_LEFTOVER_COMPLETES) && a->fc[blk] == 4096) {
+        a->fc[blk] = 0;
+        free_block(a, blk);
+      }
+    }
     if (allocation + alloc_count > 4096) allocation = ORC_FAIL;
     if (should_replace) replace_block(a, tree, slot, blk, tid);
     if (allocation != ORC_FAIL) {

@@ -23,6 +23,11 @@ extern "C" {
 /* Behaviour switches.  0 = exactly the reference.  The product fixes the
  * listed reference defects; the oracle models either side. */
 #define ORC_FIX_GATHER_EXIT_ROLLBACK 0x1u /* veb.cuh:447 spurious rollback   */
+/* block.cuh:267-281 adds a malloc's leftover slices to the free counter with
+ * no completion check; when those slices are the last ones the block was
+ * owed, the block is never returned (leaked).  With the fix the leftover
+ * credit completes the block like any other free. */
+#define ORC_FIX_LEFTOVER_COMPLETES 0x2u
 
 typedef struct orc_alloc orc_alloc;
 

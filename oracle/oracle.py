@@ -15,8 +15,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 
 FIX_GATHER_EXIT_ROLLBACK = 0x1
+FIX_LEFTOVER_COMPLETES = 0x2
 # the product fixes these reference defects; parity runs against the product use them
-PRODUCT_FIXES = FIX_GATHER_EXIT_ROLLBACK
+PRODUCT_FIXES = FIX_GATHER_EXIT_ROLLBACK | FIX_LEFTOVER_COMPLETES
 
 _lib = None
 
@@ -70,6 +71,17 @@ def gen_log_trace(seed, nops, malloc_pct, lo_bits, hi_bits):
     ops = np.zeros(nops, dtype=np.uint64)
     lib().orc_gen_trace_log(seed, nops, malloc_pct, lo_bits, hi_bits, ops.ctypes.data)
     return ops
+
+
+def gen_leftover_trace(slice_size):
+    """Fill one block of the largest size class but its last slice, free all
+    of it, then ask for a run of two slices: the run does not fit, so the one
+    slice left over is credited back (block.cuh:267-281) and completes the
+    block's free count.  Then free the run."""
+    n = 4095
+    ops = [slice_size] * n + [(1 << 63) | i for i in range(n)] + [2 * slice_size]
+    ops.append((1 << 63) | (len(ops) - 1))
+    return np.array(ops, dtype=np.uint64)
 
 
 def murmur64a(key, seed):

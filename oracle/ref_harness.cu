@@ -277,14 +277,17 @@ extern "C" __global__ void ref_export(ref_type *a, export_ptrs p) {
 }
 
 // ---- mixed-size churn through the reference's per-thread malloc/free ----
-extern "C" __global__ void ref_churn_malloc(ref_type *a, void **ptrs, uint64_t base, uint64_t n,
-                                           uint32_t seed, unsigned long long *stats) {
-  galwl::churn_malloc_body(a, ptrs, base, n, seed, stats);
+extern "C" __global__ void ref_churn_malloc(ref_type *a, void **ptrs, uint32_t *live, uint64_t base,
+                                           uint64_t n, uint32_t seed, unsigned long long *stats) {
+  galwl::churn_malloc_body(a, ptrs, live, base, n, seed, stats);
 }
 
-extern "C" __global__ void ref_churn_free(ref_type *a, void **ptrs, uint64_t nslots, uint32_t round,
-                                         uint32_t seed, int all, unsigned long long *stats) {
-  galwl::churn_free_body(a, ptrs, nslots, round, seed, all != 0, stats);
+// persistent grid of 256-thread CTAs (ref_loader.c sizes it by occupancy)
+extern "C" __global__ void __launch_bounds__(256)
+    ref_churn_free(ref_type *a, void **ptrs, uint32_t *live, uint64_t nslots, uint32_t round,
+                   uint32_t seed, int all, unsigned long long *stats) {
+  __shared__ uint16_t lists[256 / 32][galwl::WARP_SLOTS];
+  galwl::churn_free_warps(a, ptrs, live, nslots, round, seed, all != 0, stats, lists[threadIdx.x >> 5]);
 }
 
 // 1,048,576 threads x global_malloc(16) + tid stamp (tests/src/global_test.cu:34-118)

@@ -27,6 +27,7 @@
 
 static CUcontext g_ctx;
 static CUmodule g_mod;
+static unsigned g_free_grid; /* persistent grid of ref_churn_free: SMs x resident CTAs */
 static CUfunction f_build, f_boot1, f_bootr, f_replay, f_export, f_cmalloc, f_cfree, f_smalloc, f_sfree;
 static int g_open = 0;
 
@@ -53,6 +54,12 @@ int ref_open(const char *cubin) {
   CK(cuModuleGetFunction(&f_cfree, g_mod, "ref_churn_free"));
   CK(cuModuleGetFunction(&f_smalloc, g_mod, "ref_stamp_malloc"));
   CK(cuModuleGetFunction(&f_sfree, g_mod, "ref_stamp_free"));
+  {
+    int sms = 0, per_sm = 0;
+    CK(cuDeviceGetAttribute(&sms, CU_DEVICE_ATTRIBUTE_MULTIPROCESSOR_COUNT, d));
+    CK(cuOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f_cfree, 256, 0));
+    g_free_grid = (unsigned)(sms * (per_sm > 0 ? per_sm : 1));
+  }
   g_open = 1;
   return 0;
 }
@@ -185,6 +192,12 @@ int ref_export(void *h, const gal_state_dims *d, gal_state_view *v) {
   return 0;
 }
 
+/* the free phase is persistent: one warp per 1,024 slots at a time (churn.cuh) */
+static unsigned free_grid(uint64_t nscan) {
+  uint64_t need = (nscan + 8 * 1024 - 1) / (8 * 1024);
+  return (unsigned)(need < g_free_grid ? need : g_free_grid);
+}
+
 /* Mixed-size churn, `steps` timed steps after `warmup` untimed ones.  One step:
  * rounds x (50% coin frees of live slots before every round but the first,
  * then threads_per_round mallocs), then a drain of every live slot.
@@ -193,9 +206,13 @@ int ref_churn(void *h, uint64_t threads_per_round, uint32_t rounds, uint32_t see
               int steps, float *out_ms, unsigned long long *stats_out) {
   ref_inst *r = (ref_inst *)h;
   uint64_t nslots = threads_per_round * rounds;
-  CUdeviceptr ptrs, stats;
+  /* rounds are whole warps of liveness words and coin groups (churn.cuh SLOT_ALIGN) */
+  if (threads_per_round % 128) return -2;
+  CUdeviceptr ptrs, live, stats;
   CK(cuMemAlloc(&ptrs, nslots * 8));
   CK(cuMemsetD8(ptrs, 0, nslots * 8));
+  CK(cuMemAlloc(&live, nslots / 8));
+  CK(cuMemsetD8(live, 0, nslots / 8));
   CK(cuMemAlloc(&stats, 32));
   CUevent e0, e1;
   CK(cuEventCreate(&e0, CU_EVENT_DEFAULT));
@@ -208,23 +225,22 @@ int ref_churn(void *h, uint64_t threads_per_round, uint32_t rounds, uint32_t see
     CK(cuEventRecord(e0, 0));
     for (uint32_t rd = 0; rd < rounds; rd++) {
       if (rd > 0) {
-        uint64_t live = threads_per_round * rd;
+        uint64_t nscan = threads_per_round * rd;
         int all = 0;
-        void *fa[] = {&r->alloc, &ptrs, &live, &rd, &seed, &all, &stats};
-        /* the free phase gives each thread 4 consecutive slots (churn.cuh) */
-        int e = launch(f_cfree, (unsigned)((live + 4 * block - 1) / (4 * block)), block, fa);
+        void *fa[] = {&r->alloc, &ptrs, &live, &nscan, &rd, &seed, &all, &stats};
+        int e = launch(f_cfree, free_grid(nscan), block, fa);
         if (e) return e;
       }
       uint64_t base = threads_per_round * rd;
-      void *ma[] = {&r->alloc, &ptrs, &base, &threads_per_round, &seed, &stats};
+      void *ma[] = {&r->alloc, &ptrs, &live, &base, &threads_per_round, &seed, &stats};
       int e = launch(f_cmalloc, (unsigned)((threads_per_round + block - 1) / block), block, ma);
       if (e) return e;
     }
     {
       int all = 1;
       uint32_t rd = rounds;
-      void *fa[] = {&r->alloc, &ptrs, &nslots, &rd, &seed, &all, &stats};
-      int e = launch(f_cfree, (unsigned)((nslots + 4 * block - 1) / (4 * block)), block, fa);
+      void *fa[] = {&r->alloc, &ptrs, &live, &nslots, &rd, &seed, &all, &stats};
+      int e = launch(f_cfree, free_grid(nslots), block, fa);
       if (e) return e;
     }
     CK(cuEventRecord(e1, 0));
@@ -241,6 +257,7 @@ int ref_churn(void *h, uint64_t threads_per_round, uint32_t rounds, uint32_t see
   CK(cuEventDestroy(e0));
   CK(cuEventDestroy(e1));
   CK(cuMemFree(ptrs));
+  CK(cuMemFree(live));
   CK(cuMemFree(stats));
   return 0;
 }

@@ -132,6 +132,34 @@ def test_churn_payloads(G, batched):
         g.close()
 
 
+def test_churn_e2e_payloads(G, torch):
+    """The same churn through the public batched entry points, sizes copied
+    from pinned host memory every round."""
+    g = G.Gallatin.generate_on_device(16 << 30, 42)
+    try:
+        N, R = 1 << 18, 4
+        sizes = torch.empty(N * R, dtype=torch.int64, pin_memory=True)
+        sizes.numpy()[:] = G.churn_sizes(0, N * R, 1).view(np.int64)
+        ms, r = g.bench_churn_e2e(sizes.data_ptr(), N, R, 1, 1, 2)
+        assert r.mallocs_ok == 2 * N * R and r.mallocs_failed == 0
+        assert r.payload_mismatch == 0
+        assert r.frees == r.mallocs_ok
+        assert r.error_word == 0
+    finally:
+        g.close()
+
+
+def test_churn_rounds_must_align(G):
+    """Rounds are whole warps of liveness words: a round size that is not a
+    multiple of 128 requests is refused before anything launches."""
+    g = G.Gallatin.generate_on_device(2 << 30, 42)
+    try:
+        with pytest.raises(G.GalError):
+            g.bench_churn(1000, 2, 1, True, True, 0, 1)
+    finally:
+        g.close()
+
+
 def test_exhaustion_returns_null_then_recovers(G, torch):
     """Tiny arena: 4 KiB class runs dry, frees give whole segments back, and
     whole-block requests are served again."""

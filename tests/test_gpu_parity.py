@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 
 from gallatin_gb300._abi import FAIL, GAL_POLICY_LOWEST, StateView
-from oracle.oracle import PRODUCT_FIXES, Oracle, gen_log_trace, gen_serial_trace
+from oracle.oracle import PRODUCT_FIXES, Oracle, gen_leftover_trace, gen_log_trace, gen_serial_trace
 
 pytestmark = pytest.mark.gpu
 
@@ -100,6 +100,25 @@ def test_other_geometries_match_oracle(G, geom):
         o = Oracle(4 << 30, 3, bytes_per_segment=seg, min_size=mn, max_size=mx, fixes=PRODUCT_FIXES)
         np.testing.assert_array_equal(out, o.replay(ops, smid=smid))
         assert g.export().diff(o.export()) == []
+    finally:
+        g.close()
+
+
+@pytest.mark.parametrize("max_size", [4096, 1024])
+def test_leftover_credit_completes_block(G, max_size):
+    """A run that does not fit credits its leftover slices; when they are the
+    last the block was owed, the block goes back to its segment (the
+    reference leaks it, block.cuh:267-281)."""
+    ops = gen_leftover_trace(max_size)
+    g = G.Gallatin.generate_on_device(1 << 30, 5, max_size=max_size)
+    try:
+        out, smid = g.replay(ops)
+        o = Oracle(1 << 30, 5, max_size=max_size, fixes=PRODUCT_FIXES)
+        np.testing.assert_array_equal(out, o.replay(ops, smid=smid))
+        sv = g.export()
+        assert sv.diff(o.export()) == []
+        assert (sv.free_counters < 4096).all()
+        assert g.error_word() == 0
     finally:
         g.close()
 
