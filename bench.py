@@ -52,7 +52,7 @@ WORKLOAD = ("mixed-size churn: arena 128 GiB (8192 x 16 MiB segments, Gallatin<1
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--steps", type=int, default=30)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--threads-per-round", type=int, default=N_PER_ROUND)
@@ -90,9 +90,15 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # start timing only once the sampler is live (its first row is out),
+            # then drop that row: it was taken before the timed region
+            t0 = time.time()
+            while not self.rows and time.time() - t0 < 5:
+                time.sleep(0.005)
+            self.rows.clear()
         except FileNotFoundError:
             self.proc = None
         return self

@@ -88,6 +88,8 @@ def lib():
         "gal_free_per_thread": ([vp, vp, u64, vp], C.c_int),
         "gal_malloc_batched": ([vp, vp, u64, vp, vp], C.c_int),
         "gal_free_batched": ([vp, vp, u64, vp], C.c_int),
+        "gal_free_batched_n": ([vp, vp, vp, u64, vp], C.c_int),
+        "gal_trim": ([vp, vp], C.c_int),
         "gal_bench_churn": ([vp, u64, u32, u32, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp], C.c_int),
         "gal_bench_churn_e2e": ([vp, vp, u64, u32, u32, C.c_int, C.c_int, vp, vp], C.c_int),
         "gal_churn_sizes": ([u64, u64, u32, vp], C.c_int),
@@ -258,6 +260,16 @@ class Gallatin:
 
     def free_batched(self, ptrs, stream=None):
         _check(lib().gal_free_batched(self._h, _ptr(ptrs), ptrs.numel(), stream), "gal_free_batched")
+
+    def trim(self, stream=None):
+        """Retire the pinned blocks and boot the slots again (quiescent only)."""
+        _check(lib().gal_trim(self._h, stream), "gal_trim")
+
+    def free_batched_n(self, ptrs, d_count, stream=None):
+        """Free the first d_count[0] entries of ptrs (a one-element uint64/int64
+        device tensor written by earlier work on the stream)."""
+        _check(lib().gal_free_batched_n(self._h, _ptr(ptrs), _ptr(d_count), ptrs.numel(), stream),
+               "gal_free_batched_n")
 
     def bench_churn(self, threads_per_round, rounds, seed, batched, use_graph, warmup, steps):
         """batched: True/False, or a mask (1: CTA-aggregated malloc, 2: CTA-aggregated free)."""

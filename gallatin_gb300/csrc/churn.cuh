@@ -130,56 +130,108 @@ __device__ __forceinline__ void clear_live(uint32_t *live_bits, uint64_t i0, uin
 constexpr int WARP_WORDS = 32;
 constexpr int WARP_SLOTS = 32 * WARP_WORDS;
 
+// One warp's 1,024 slots from word w0: reads and clears the liveness words of
+// the slots it selects and lists the selected slots (offsets from w0 * 32) in
+// slot order; returns how many.  Full warp.
+__device__ __forceinline__ uint32_t list_selected(uint32_t *live_bits, uint64_t words, uint64_t w0,
+                                                  uint32_t round, uint32_t seed, bool all,
+                                                  uint16_t *list) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint64_t w = w0 + lane;
+  const uint32_t word = w < words ? live_bits[w] : 0u;
+  uint32_t sel = word;
+  if (sel && !all) sel &= free_coin_group(w >> 2, round, seed).v[w & 3u];
+  if (sel) live_bits[w] = word & ~sel;
+  const uint32_t n = (uint32_t)__popc(sel);
+  uint32_t end = n;  // inclusive scan of the counts
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t v = __shfl_up_sync(0xFFFFFFFFu, end, o);
+    if ((int)lane >= o) end += v;
+  }
+  uint32_t pos = end - n;
+  for (uint32_t b = sel; b; b &= b - 1u) list[pos++] = (uint16_t)(lane * 32u + (uint32_t)__ffs(b) - 1u);
+  __syncwarp();
+  return __shfl_sync(0xFFFFFFFFu, end, 31);
+}
+
+// Pointers and payload words of list entries j0 + k*32 + lane (k < FREE_SLOTS),
+// loads issued together; go[k] marks the entries that exist.
+__device__ __forceinline__ void load_listed(void **ptrs, uint64_t w0, const uint16_t *list,
+                                            uint32_t total, uint32_t j0, uint32_t seed, void **p,
+                                            bool *go, uint32_t &nbad, uint32_t &ngo) {
+  const uint32_t lane = threadIdx.x & 31u;
+  uint64_t slot[FREE_SLOTS];
+  uint32_t seen[FREE_SLOTS];
+#pragma unroll
+  for (int k = 0; k < FREE_SLOTS; k++) {
+    const uint32_t j = j0 + (uint32_t)k * 32u + lane;
+    slot[k] = j < total ? w0 * 32u + list[j] : 0;
+    p[k] = j < total ? ptrs[slot[k]] : nullptr;
+  }
+#pragma unroll
+  for (int k = 0; k < FREE_SLOTS; k++) {
+    go[k] = p[k] != nullptr;
+    seen[k] = go[k] ? *(const uint32_t *)p[k] : 0u;
+  }
+#pragma unroll
+  for (int k = 0; k < FREE_SLOTS; k++)
+    if (go[k]) {
+      nbad += seen[k] != payload(slot[k], seed);
+      ngo++;
+    }
+}
+
 template <class Alloc>
 __device__ __forceinline__ void churn_free_warps(Alloc *a, void **ptrs, uint32_t *live_bits,
                                                  uint64_t nslots, uint32_t round, uint32_t seed,
                                                  bool all, unsigned long long *stats,
                                                  uint16_t *list /* WARP_SLOTS entries */) {
+  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint64_t words = nslots >> 5;
+  uint32_t nbad = 0, ngo = 0;
+  for (uint64_t w0 = warp * WARP_WORDS; w0 < words; w0 += nwarps * WARP_WORDS) {
+    const uint32_t total = list_selected(live_bits, words, w0, round, seed, all, list);
+    for (uint32_t j0 = 0; j0 < total; j0 += 32u * FREE_SLOTS) {
+      void *p[FREE_SLOTS];
+      bool go[FREE_SLOTS];
+      load_listed(ptrs, w0, list, total, j0, seed, p, go, nbad, ngo);
+      free_many<Alloc>::run(a, p, go);
+    }
+    __syncwarp();
+  }
+  warp_add(&stats[2], nbad);
+  warp_add(&stats[3], ngo);
+}
+
+// The same selection, but the selected pointers are appended to freelist
+// (*count entries so far; one atomicAdd per warp and chunk) for a batched
+// free call to serve; payloads are checked here.
+__device__ __forceinline__ void churn_select_warps(void **ptrs, uint32_t *live_bits, uint64_t nslots,
+                                                   uint32_t round, uint32_t seed, bool all,
+                                                   unsigned long long *stats, uint16_t *list,
+                                                   void **freelist, unsigned long long *count) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   const uint64_t words = nslots >> 5;
   uint32_t nbad = 0, ngo = 0;
   for (uint64_t w0 = warp * WARP_WORDS; w0 < words; w0 += nwarps * WARP_WORDS) {
-    const uint64_t w = w0 + lane;
-    const uint32_t word = w < words ? live_bits[w] : 0u;
-    uint32_t sel = word;
-    if (sel && !all) sel &= free_coin_group(w >> 2, round, seed).v[w & 3u];
-    if (sel) live_bits[w] = word & ~sel;
-    const uint32_t n = (uint32_t)__popc(sel);
-    uint32_t end = n;  // inclusive scan of the counts
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      uint32_t v = __shfl_up_sync(0xFFFFFFFFu, end, o);
-      if ((int)lane >= o) end += v;
-    }
-    const uint32_t total = __shfl_sync(0xFFFFFFFFu, end, 31);
-    uint32_t pos = end - n;
-    for (uint32_t b = sel; b; b &= b - 1u) list[pos++] = (uint16_t)(lane * 32u + (uint32_t)__ffs(b) - 1u);
-    __syncwarp();
+    const uint32_t total = list_selected(live_bits, words, w0, round, seed, all, list);
+    if (total == 0) continue;  // warp-uniform
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(count, (unsigned long long)total);
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
     for (uint32_t j0 = 0; j0 < total; j0 += 32u * FREE_SLOTS) {
       void *p[FREE_SLOTS];
       bool go[FREE_SLOTS];
-      uint64_t slot[FREE_SLOTS];
-      uint32_t seen[FREE_SLOTS];
+      load_listed(ptrs, w0, list, total, j0, seed, p, go, nbad, ngo);
 #pragma unroll
       for (int k = 0; k < FREE_SLOTS; k++) {
         const uint32_t j = j0 + (uint32_t)k * 32u + lane;
-        slot[k] = j < total ? w0 * 32u + list[j] : 0;
-        p[k] = j < total ? ptrs[slot[k]] : nullptr;
+        if (j < total) freelist[base + j] = p[k];
       }
-#pragma unroll
-      for (int k = 0; k < FREE_SLOTS; k++) {
-        go[k] = p[k] != nullptr;
-        seen[k] = go[k] ? *(const uint32_t *)p[k] : 0u;  // loads in flight together
-      }
-#pragma unroll
-      for (int k = 0; k < FREE_SLOTS; k++)
-        if (go[k]) {
-          nbad += seen[k] != payload(slot[k], seed);
-          ngo++;
-        }
-      free_many<Alloc>::run(a, p, go);
     }
     __syncwarp();
   }

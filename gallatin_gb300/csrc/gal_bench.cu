@@ -139,38 +139,15 @@ __global__ void k_stamp_payload(void **ptrs, uint32_t *live, uint64_t base, uint
   galwl::warp_count(&stats[1], p == nullptr);
 }
 
-// freelist[i] = the pointer of slot i when it is freed this round, else null
-__global__ void k_select_frees(void **ptrs, uint32_t *live, void **freelist, uint64_t nslots,
-                               uint32_t round, uint32_t seed, int all, unsigned long long *stats) {
-  constexpr int F = galwl::FREE_SLOTS;
-  uint64_t i0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * F;
-  if (i0 >= nslots) return;  // whole warps: nslots is a multiple of SLOT_ALIGN
-  const uint32_t word = live[i0 >> 5];
-  const uint32_t sel = galwl::select_frees(word, i0, round, seed, all != 0);
-  void *p[F];
-  if (sel) {
-    galwl::load_slots(ptrs, i0, nslots, p);
-  } else {
-#pragma unroll
-    for (int k = 0; k < F; k++) p[k] = nullptr;
-  }
-  uint32_t nbad = 0, ngo = 0;
-#pragma unroll
-  for (int k = 0; k < F; k++) {
-    bool go = ((sel >> k) & 1u) && p[k] != nullptr;
-    if (go) {
-      nbad += *(const uint32_t *)p[k] != galwl::payload(i0 + k, seed);
-      ngo++;
-    } else {
-      p[k] = nullptr;
-    }
-  }
-#pragma unroll
-  for (int k = 0; k < F; k += 2)
-    *(ulonglong2 *)(freelist + i0 + k) = make_ulonglong2((unsigned long long)p[k], (unsigned long long)p[k + 1]);
-  galwl::clear_live(live, i0, word, sel);
-  galwl::warp_add(&stats[2], nbad);
-  galwl::warp_add(&stats[3], ngo);
+// Appends the pointers this round frees to freelist (*count entries so far)
+// and checks their payloads; persistent grid, one warp per 1,024 slots.
+__global__ void __launch_bounds__(FREE_BT)
+    k_select_free_list(void **ptrs, uint32_t *live, void **freelist, unsigned long long *count,
+                       uint64_t nslots, uint32_t round, uint32_t seed, int all,
+                       unsigned long long *stats) {
+  __shared__ uint16_t lists[FREE_BT / 32][galwl::WARP_SLOTS];
+  galwl::churn_select_warps(ptrs, live, nslots, round, seed, all != 0, stats, lists[threadIdx.x >> 5],
+                            freelist, count);
 }
 
 // n threads x malloc(size) + thread-id stamp, then check + free (global_test.cu)
@@ -245,14 +222,16 @@ __global__ void __launch_bounds__(BT)
   }
 }
 
+// the batched free path (gal_free_batched): warp teams per block through
+// gal::free_n, here one pointer per thread so each free is timed alone
 __global__ void __launch_bounds__(BT)
     k_lat_free_batched(const gal::state *s, void **ptrs, uint64_t base, uint64_t n, uint32_t *cycles) {
-  __shared__ gal::cta_free_smem<2 * BT> sm;
   for (uint64_t c = (uint64_t)blockIdx.x * BT; c < n; c += (uint64_t)gridDim.x * BT) {
     uint64_t t = c + threadIdx.x;
-    void *p = t < n ? ptrs[base + t] : nullptr;
+    void *const p[1] = {t < n ? ptrs[base + t] : nullptr};
+    const bool go[1] = {p[0] != nullptr};
     long long c0 = clock64();
-    gal::cta_free<2 * BT>(s, p, sm);
+    gal::free_n<1>(s, p, go);
     long long c1 = clock64();
     if (t < n) {
       ptrs[base + t] = nullptr;
@@ -458,9 +437,11 @@ done:
 
 /* The churn end to end through the public entry points: every round the
  * request sizes are copied from pinned host memory (host_sizes, rounds x
- * threads_per_round, same sizes as the device-generated workload), served by
- * gal_malloc_batched, stamped by a user kernel; frees are selected by a user
- * kernel and served by gal_free_batched; the step's counters are read back. */
+ * threads_per_round, same sizes as the device-generated workload) on a copy
+ * stream, two rounds ahead into two alternating buffers, and served by
+ * gal_malloc_batched; a user kernel stamps the payloads; frees are selected by
+ * a user kernel that compacts them into a list whose length stays on the
+ * device, served by gal_free_batched_n; the step's counters are read back. */
 int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t threads_per_round,
                         uint32_t rounds, uint32_t seed, int warmup, int steps, float *step_ms,
                         gal_churn_result *res) {
@@ -470,41 +451,67 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
   const uint64_t N = threads_per_round, nslots = N * rounds;
   void **ptrs = nullptr, **freelist = nullptr;
   uint32_t *live = nullptr;
-  uint64_t *d_sizes = nullptr;
-  unsigned long long *stats = nullptr;
+  uint64_t *d_sizes[2] = {nullptr, nullptr};
+  unsigned long long *stats = nullptr, *count = nullptr;
   unsigned long long hst[4];
-  cudaStream_t st = nullptr;
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaStream_t st = nullptr, cp = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr, copied[2] = {nullptr, nullptr}, consumed[2] = {nullptr, nullptr};
+  int dev = 0, sms = 0, per_sm = 0;
   memset(res, 0, sizeof(*res));
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_select_free_list, FREE_BT, 0);
+  const uint64_t grid_sel = (uint64_t)sms * (per_sm > 0 ? per_sm : 1);
   CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&cp, cudaStreamNonBlocking));
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
+  for (int b = 0; b < 2; b++) {
+    CK(cudaEventCreateWithFlags(&copied[b], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&consumed[b], cudaEventDisableTiming));
+    CK(cudaMalloc(&d_sizes[b], N * sizeof(uint64_t)));
+  }
   CK(cudaMalloc(&ptrs, nslots * sizeof(void *)));
   CK(cudaMalloc(&freelist, nslots * sizeof(void *)));
-  CK(cudaMalloc(&d_sizes, N * sizeof(uint64_t)));
-  CK(cudaMalloc(&stats, 4 * sizeof(unsigned long long)));
-  CK(cudaMemsetAsync(ptrs, 0, nslots * sizeof(void *), st));
   CK(cudaMalloc(&live, nslots / 8));
+  CK(cudaMalloc(&stats, 4 * sizeof(unsigned long long)));
+  CK(cudaMalloc(&count, sizeof(unsigned long long)));
+  CK(cudaMemsetAsync(ptrs, 0, nslots * sizeof(void *), st));
   CK(cudaMemsetAsync(live, 0, nslots / 8, st));
   for (int s = 0; s < warmup + steps; s++) {
     CK(cudaStreamSynchronize(st));
     CK(cudaEventRecord(e0, st));
+    CK(cudaStreamWaitEvent(cp, e0, 0));
+    for (uint32_t r = 0; r < rounds && r < 2; r++) {
+      CK(cudaMemcpyAsync(d_sizes[r], host_sizes + (uint64_t)r * N, N * sizeof(uint64_t),
+                         cudaMemcpyHostToDevice, cp));
+      CK(cudaEventRecord(copied[r], cp));
+    }
     CK(cudaMemsetAsync(stats, 0, sizeof(hst), st));
     for (uint32_t r = 0; r <= rounds; r++) {
       bool drain = r == rounds;
       if (r > 0) {
         uint64_t nscan = drain ? nslots : N * r;
-        const uint64_t nt = (nscan + galwl::FREE_SLOTS - 1) / galwl::FREE_SLOTS;
-        k_select_frees<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(ptrs, live, freelist, nscan, r, seed,
-                                                                      drain ? 1 : 0, stats);
-        int e = gal_free_batched(h, freelist, nscan, st);
+        const uint64_t chunk = (uint64_t)(FREE_BT / 32) * galwl::WARP_SLOTS;
+        unsigned g = (unsigned)std::min<uint64_t>((nscan + chunk - 1) / chunk, grid_sel);
+        CK(cudaMemsetAsync(count, 0, sizeof(unsigned long long), st));
+        k_select_free_list<<<g, FREE_BT, 0, st>>>(ptrs, live, freelist, count, nscan, r, seed,
+                                                  drain ? 1 : 0, stats);
+        int e = gal_free_batched_n(h, freelist, count, nscan, st);
         if (e) { rc = e; goto done; }
       }
       if (drain) break;
-      CK(cudaMemcpyAsync(d_sizes, host_sizes + (uint64_t)r * N, N * sizeof(uint64_t),
-                         cudaMemcpyHostToDevice, st));
-      int e = gal_malloc_batched(h, d_sizes, N, ptrs + (uint64_t)r * N, st);
+      const int b = (int)(r & 1u);
+      CK(cudaStreamWaitEvent(st, copied[b], 0));
+      int e = gal_malloc_batched(h, d_sizes[b], N, ptrs + (uint64_t)r * N, st);
       if (e) { rc = e; goto done; }
+      CK(cudaEventRecord(consumed[b], st));
+      if (r + 2 < rounds) {  // refill this buffer with round r + 2 while the GPU works
+        CK(cudaStreamWaitEvent(cp, consumed[b], 0));
+        CK(cudaMemcpyAsync(d_sizes[b], host_sizes + (uint64_t)(r + 2) * N, N * sizeof(uint64_t),
+                           cudaMemcpyHostToDevice, cp));
+        CK(cudaEventRecord(copied[b], cp));
+      }
       k_stamp_payload<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(ptrs, live, (uint64_t)r * N, N, seed,
                                                                    stats);
     }
@@ -530,14 +537,22 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
   res->d2h_bytes = sizeof(hst);
   gal_last_error(h, &res->error_word);
 done:
+  if (st) cudaStreamSynchronize(st);
+  if (cp) cudaStreamSynchronize(cp);
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
+  for (int b = 0; b < 2; b++) {
+    if (copied[b]) cudaEventDestroy(copied[b]);
+    if (consumed[b]) cudaEventDestroy(consumed[b]);
+    if (d_sizes[b]) cudaFree(d_sizes[b]);
+  }
   if (ptrs) cudaFree(ptrs);
   if (live) cudaFree(live);
   if (freelist) cudaFree(freelist);
-  if (d_sizes) cudaFree(d_sizes);
   if (stats) cudaFree(stats);
+  if (count) cudaFree(count);
   if (st) cudaStreamDestroy(st);
+  if (cp) cudaStreamDestroy(cp);
   return rc;
 }
 

@@ -71,6 +71,38 @@ __global__ void k_boot(const gal::state *s) {
       if (!gal::boot_block(s, t, i, 0)) gal::set_error(s, GAL_DEV_ERR_BOOT);
 }
 
+// gal_trim: retire every pinned block (slot order, one thread), crediting the
+// slices it never handed out so that a block with nothing live goes back to
+// its segment now (and one with live slices when the last is freed), then
+// boot the slots again in the one-thread order.
+__global__ void k_trim(const gal::state *s) {
+  if (threadIdx.x + blockIdx.x * blockDim.x != 0) return;
+  for (uint32_t t = 0; t < s->num_trees; t++)
+    for (uint32_t i = 0; i < s->slot_count[t]; i++) {
+      uint32_t blk = atomicExch(s->slots + s->slot_base[t] + i, gal::NOBLK);
+      if (blk == gal::NOBLK) continue;
+      unsigned long long old = atomicAdd(&s->mwords[blk], (unsigned long long)gal::SLICES_PER_BLOCK);
+      uint32_t handed_out = (uint32_t)old;
+      if (handed_out < gal::SLICES_PER_BLOCK) gal::credit_frees(s, blk, gal::SLICES_PER_BLOCK - handed_out);
+    }
+  // segments of a class none of whose blocks is out (those gathered ahead when
+  // a class took the last block of its previous segment) go back too
+  for (uint64_t seg = 0; seg < s->num_segments; seg++) {
+    uint16_t tree = s->tree_ids[seg];
+    if (tree >= s->num_trees) continue;
+    int idle = (int)gal::blocks_in_segment(s, tree) - 1;
+    if (atomicCAS(&s->active[seg], idle, -1) != idle) continue;
+    gal::veb_remove(gal::sub_tree(s, tree), seg);
+    __threadfence();
+    if (gal::cas16(&s->tree_ids[seg], tree, gal::FREE_TREE) != tree) gal::set_error(s, GAL_DEV_ERR_SEGMENT_SETUP);
+    __threadfence();
+    gal::veb_insert(gal::seg_tree(s), seg);
+  }
+  for (uint32_t t = 0; t < s->num_trees; t++)
+    for (uint32_t i = 0; i < s->slot_count[t]; i++)
+      if (!gal::boot_block(s, t, i, 0)) gal::set_error(s, GAL_DEV_ERR_BOOT);
+}
+
 __global__ void k_export_blocks(const gal::state *s, uint32_t *mc, uint64_t nblocks) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -183,21 +215,37 @@ __global__ void __launch_bounds__(BATCH_THREADS)
   }
 }
 
+// Batched free: each thread takes FREE_PER_THREAD consecutive entries per
+// pass of a persistent grid and frees them with gal::free_n (table lookups and
+// free-counter atomics issued back to back, warp teams per block).  The list
+// holds n entries, or *d_count when that is given and smaller (a count that
+// an earlier kernel on the stream wrote).
+constexpr int FREE_PER_THREAD = 4;
+
 __global__ void __launch_bounds__(BATCH_THREADS)
-    k_free_batched(const gal::state *s, void *const *ptrs, uint64_t n) {
-  __shared__ gal::cta_free_smem<2 * BATCH_THREADS> sm;
-  for (uint64_t base = (uint64_t)blockIdx.x * BATCH_THREADS; base < n;
-       base += (uint64_t)gridDim.x * BATCH_THREADS) {
-    uint64_t i = base + threadIdx.x;
-    gal::cta_free<2 * BATCH_THREADS>(s, i < n ? ptrs[i] : nullptr, sm);
+    k_free_batched(const gal::state *s, void *const *ptrs, uint64_t n,
+                   const unsigned long long *d_count) {
+  if (d_count && *d_count < n) n = *d_count;
+  const uint64_t stride = (uint64_t)gridDim.x * BATCH_THREADS * FREE_PER_THREAD;
+  for (uint64_t i0 = ((uint64_t)blockIdx.x * BATCH_THREADS + threadIdx.x) * FREE_PER_THREAD; i0 < n;
+       i0 += stride) {
+    void *p[FREE_PER_THREAD];
+    bool go[FREE_PER_THREAD];
+#pragma unroll
+    for (int k = 0; k < FREE_PER_THREAD; k++) {
+      p[k] = i0 + k < n ? ptrs[i0 + k] : nullptr;
+      go[k] = p[k] != nullptr;
+    }
+    gal::free_n<FREE_PER_THREAD>(s, p, go);
   }
 }
 
-int persistent_grid(int device) {
+template <class K>
+int persistent_grid(int device, K kernel) {
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_malloc_batched, BATCH_THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, BATCH_THREADS, 0);
   if (per_sm < 1) per_sm = 1;
   return sms * per_sm;
 }
@@ -606,22 +654,35 @@ int gal_free_per_thread(gal_handle *h, void *const *ptrs, uint64_t n, void *stre
   return GAL_OK;
 }
 
+int gal_trim(gal_handle *h, void *stream) {
+  if (!h) return GAL_ERR_ARGS;
+  k_trim<<<1, 1, 0, (cudaStream_t)stream>>>(h->d_state);
+  CUDA_TRY(cudaGetLastError());
+  return GAL_OK;
+}
+
 int gal_malloc_batched(gal_handle *h, const uint64_t *sizes, uint64_t n, void **out, void *stream) {
   if (!h || (n && (!sizes || !out))) return GAL_ERR_ARGS;
   if (!n) return GAL_OK;
   unsigned g = grid_for(n, BATCH_THREADS);
-  unsigned p = (unsigned)persistent_grid(h->device);
+  unsigned p = (unsigned)persistent_grid(h->device, k_malloc_batched);
   k_malloc_batched<<<g < p ? g : p, BATCH_THREADS, 0, (cudaStream_t)stream>>>(h->d_state, sizes, n, out);
   CUDA_TRY(cudaGetLastError());
   return GAL_OK;
 }
 
 int gal_free_batched(gal_handle *h, void *const *ptrs, uint64_t n, void *stream) {
-  if (!h || (n && !ptrs)) return GAL_ERR_ARGS;
-  if (!n) return GAL_OK;
-  unsigned g = grid_for(n, BATCH_THREADS);
-  unsigned p = (unsigned)persistent_grid(h->device);
-  k_free_batched<<<g < p ? g : p, BATCH_THREADS, 0, (cudaStream_t)stream>>>(h->d_state, ptrs, n);
+  return gal_free_batched_n(h, ptrs, nullptr, n, stream);
+}
+
+int gal_free_batched_n(gal_handle *h, void *const *ptrs, const unsigned long long *d_count,
+                       uint64_t max_n, void *stream) {
+  if (!h || (max_n && !ptrs)) return GAL_ERR_ARGS;
+  if (!max_n) return GAL_OK;
+  unsigned g = grid_for((max_n + FREE_PER_THREAD - 1) / FREE_PER_THREAD, BATCH_THREADS);
+  unsigned p = (unsigned)persistent_grid(h->device, k_free_batched);
+  k_free_batched<<<g < p ? g : p, BATCH_THREADS, 0, (cudaStream_t)stream>>>(h->d_state, ptrs, max_n,
+                                                                            d_count);
   CUDA_TRY(cudaGetLastError());
   return GAL_OK;
 }

@@ -208,11 +208,29 @@ int gal_malloc_per_thread(gal_handle *h, const uint64_t *sizes, uint64_t n,
  * (global_free, global_allocator.cuh:78-82). */
 int gal_free_per_thread(gal_handle *h, void *const *ptrs, uint64_t n, void *stream);
 
-/* Batched form: the same results contract as gal_malloc_per_thread, served by
- * CTA-level aggregation (one claim per size class per CTA). */
+/* Give back what the pinned slots hold (no counterpart in the reference; the
+ * host-side analogue of malloc_trim).  Call with no device malloc/free in
+ * flight.  Every pinned block is retired: the slices it never handed out are
+ * credited to its free counter, so a block with nothing live returns to its
+ * segment (and one with live slices when the last of them is freed), and
+ * emptied segments return to the segment tree.  The slots are then booted
+ * again in the one-thread order, so with nothing live the trees, segment
+ * classes and slots equal those of a freshly created allocator. */
+int gal_trim(gal_handle *h, void *stream);
+
+/* Batched form: the same results contract as gal_malloc_per_thread /
+ * gal_free_per_thread.  Mallocs are served by CTA-level aggregation (one claim
+ * per size class per CTA of a persistent grid); frees four entries per thread,
+ * warp teams per block (one free-counter atomic per team). */
 int gal_malloc_batched(gal_handle *h, const uint64_t *sizes, uint64_t n,
                        void **out_ptrs, void *stream);
 int gal_free_batched(gal_handle *h, void *const *ptrs, uint64_t n, void *stream);
+/* gal_free_batched over the first *d_count entries of ptrs (at most max_n),
+ * where d_count is device memory written by earlier work on the same stream:
+ * a kernel that compacts the pointers it wants freed need not send the count
+ * back to the host first. */
+int gal_free_batched_n(gal_handle *h, void *const *ptrs, const unsigned long long *d_count,
+                       uint64_t max_n, void *stream);
 
 /* ---- served jobs (request loop, gallatin_gb300/serve.py) -------------------
  * One job = one CTA launched on `stream` that allocates through the device

@@ -610,6 +610,41 @@ static void free_offset(orc_alloc *a, uint64_t offset) {
   }
 }
 
+/* Trim (an addition of the product, gal_trim; the reference has none):
+ * retire every pinned block in slot order, crediting the slices it never
+ * handed out so that a block with nothing live goes back to its segment, then
+ * boot the slots again in the one-thread order. */
+int orc_trim(orc_alloc *a) {
+  for (int tree = 0; tree < a->num_trees; tree++)
+    for (int i = 0; i < a->nslots[tree]; i++) {
+      int32_t blk = a->slots[tree][i];
+      if (blk == NOBLK) continue;
+      a->slots[tree][i] = NOBLK;
+      uint32_t merged = a->mc[blk];
+      a->mc[blk] = merged + 4096u;
+      uint32_t c = merged & 0xFFFFFu;
+      if (c < 4096u) {
+        a->fc[blk] += 4096u - c;
+        if (a->fc[blk] == 4096u) {
+          a->fc[blk] = 0;
+          free_block(a, blk);
+        }
+      }
+    }
+  /* segments of a class none of whose blocks is out (those gathered ahead
+   * when a class took the last block of its previous segment) go back too */
+  for (uint64_t seg = 0; seg < a->S; seg++) {
+    int tree = a->tree_ids[seg];
+    if (tree >= a->num_trees) continue;
+    if (a->active[seg] != (int32_t)(blocks_per_segment_tree(a, tree) - 1)) continue;
+    a->active[seg] = -1;
+    veb_remove(&a->sub[tree], seg);
+    a->tree_ids[seg] = 0xFFFF;
+    veb_insert_force(&a->seg_tree, seg);
+  }
+  return orc_boot_one_thread(a);
+}
+
 /* pinned slot choice (shared_block_storage.cuh:119-134) */
 static int valid_block_index(orc_alloc *a, int tree, uint32_t smid) {
   int n = a->nslots[tree];

@@ -39,6 +39,9 @@ void orc_destroy(orc_alloc *a);
 /* boot_shared_block_container_one_thread (gallatin.cuh:196-221), thread id 0 */
 int orc_boot_one_thread(orc_alloc *a);
 
+/* retire every pinned block, then boot the slots again (gal_trim) */
+int orc_trim(orc_alloc *a);
+
 /* device malloc/free of one thread; offsets are byte offsets from the arena
  * base, ORC_FAIL for nullptr. */
 uint64_t orc_malloc(orc_alloc *a, uint64_t size, uint32_t smid, uint64_t tid);

@@ -40,6 +40,7 @@ def lib():
                                  C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]
         L.orc_destroy.argtypes = [C.c_void_p]
         L.orc_boot_one_thread.argtypes = [C.c_void_p]
+        L.orc_trim.argtypes = [C.c_void_p]
         L.orc_malloc.restype = C.c_uint64
         L.orc_malloc.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint64]
         L.orc_free.argtypes = [C.c_void_p, C.c_uint64]
@@ -114,6 +115,12 @@ class Oracle:
 
     def malloc(self, size, smid=0, tid=0):
         return int(lib().orc_malloc(self._h, size, smid, tid))
+
+    def trim(self):
+        """Retire every pinned block, then boot the slots again (gal_trim)."""
+        r = lib().orc_trim(self._h)
+        if r != 0:
+            raise RuntimeError(f"oracle trim failed ({r})")
 
     def free(self, byte_offset):
         lib().orc_free(self._h, byte_offset)

@@ -149,6 +149,74 @@ def test_churn_e2e_payloads(G, torch):
         g.close()
 
 
+def test_free_batched_n_stops_at_device_count(G, torch):
+    """gal_free_batched_n frees exactly the first *d_count entries: the rest of
+    the list (the odd half) is freed afterwards by gal_free_batched, which
+    would be a double free had the count been ignored."""
+    n = 1 << 18
+    g = G.Gallatin.generate_on_device(2 << 30, 42)
+    try:
+        sizes = torch.full((n,), 64, dtype=torch.int64, device="cuda")
+        ptrs = torch.zeros(n, dtype=torch.int64, device="cuda")
+        g.malloc_batched(sizes, ptrs)
+        even, odd = ptrs[0::2].contiguous(), ptrs[1::2].contiguous()
+        lst = torch.cat([even, odd])
+        cnt = torch.tensor([even.numel()], dtype=torch.int64, device="cuda")
+        g.free_batched_n(lst, cnt)
+        torch.cuda.synchronize()
+        assert g.error_word() == 0, g.error_info()
+        g.free_batched(odd)
+        torch.cuda.synchronize()
+        assert g.error_word() == 0, g.error_info()
+        sv = g.export()
+        assert (sv.free_counters <= 4096).all()
+    finally:
+        g.close()
+
+
+TREE_FIELDS = ["seg_tree_words", "sub_tree_words", "tree_ids", "slots", "free_counters"]
+
+
+@pytest.mark.parametrize("batched", [False, True])
+def test_everything_freed_then_trim_gives_fresh_trees(G, torch, batched):
+    """Concurrent mixed slice, block and segment requests, all freed, then
+    gal_trim: the vEB trees, segment classes, pinned slots and free counters
+    are word for word those of a freshly created allocator."""
+    n = 1 << 18
+    rng = np.random.default_rng(11)
+    sizes = (2 ** rng.uniform(4, 12, n)).astype(np.int64)
+    sizes[::997] = (2 ** rng.uniform(13, 26, sizes[::997].size)).astype(np.int64)
+    g = G.Gallatin.generate_on_device(16 << 30, 42)
+    try:
+        fresh = g.export()
+        d_sizes = torch.from_numpy(sizes).cuda()
+        d_ptrs = torch.zeros(n, dtype=torch.int64, device="cuda")
+        (g.malloc_batched if batched else g.malloc_per_thread)(d_sizes, d_ptrs)
+        torch.cuda.synchronize()
+        assert (d_ptrs.cpu().numpy() != 0).all()
+        (g.free_batched if batched else g.free_per_thread)(d_ptrs)
+        torch.cuda.synchronize()
+        g.trim()
+        torch.cuda.synchronize()
+        assert g.error_word() == 0, g.error_info()
+        assert g.export().diff(fresh, fields=TREE_FIELDS) == []
+    finally:
+        g.close()
+
+
+def test_churn_then_trim_gives_fresh_trees(G):
+    """The batched churn drains every allocation; after trim nothing of it remains."""
+    g = G.Gallatin.generate_on_device(16 << 30, 42)
+    try:
+        fresh = g.export()
+        ms, r = g.bench_churn(1 << 18, 4, 1, True, True, 0, 1)
+        assert r.frees == r.mallocs_ok and r.error_word == 0
+        g.trim()
+        assert g.export().diff(fresh, fields=TREE_FIELDS) == []
+    finally:
+        g.close()
+
+
 def test_churn_rounds_must_align(G):
     """Rounds are whole warps of liveness words: a round size that is not a
     multiple of 128 requests is refused before anything launches."""

@@ -136,3 +136,39 @@ def test_state_roundtrip_export_import(G):
             h.close()
     finally:
         g.close()
+
+
+def _free_everything(ops):
+    live = set()
+    for i, op in enumerate(ops):
+        if int(op) >> 63:
+            live.discard(int(op) & ~(1 << 63))
+        else:
+            live.add(i)
+    tail = np.array([(1 << 63) | i for i in sorted(live)], dtype=np.uint64)
+    return np.concatenate([np.asarray(ops, dtype=np.uint64), tail])
+
+
+@pytest.mark.parametrize("mk,nbytes", [
+    (lambda: gen_serial_trace(101, 20000, 55, 16, 256), 2 << 30),
+    (lambda: gen_log_trace(404, 4000, 55, 4, 26), 16 << 30),
+], ids=["serial", "log_big"])
+def test_trim_matches_oracle_and_fresh_state(G, mk, nbytes):
+    """Free everything, trim: the whole state equals the oracle's, and the
+    trees, segment classes, slots and free counters equal a fresh allocator's."""
+    ops = _free_everything(mk())
+    g = G.Gallatin.generate_on_device(nbytes, 42)
+    try:
+        fresh = g.export()
+        out, smid = g.replay(ops)
+        g.trim()
+        o = Oracle(nbytes, 42, fixes=PRODUCT_FIXES)
+        np.testing.assert_array_equal(out, o.replay(ops, smid=smid))
+        o.trim()
+        sv = g.export()
+        assert sv.diff(o.export()) == []
+        assert sv.diff(fresh, fields=["seg_tree_words", "sub_tree_words", "tree_ids", "slots",
+                                      "free_counters"]) == []
+        assert g.error_word() == 0
+    finally:
+        g.close()

@@ -11,7 +11,7 @@ import pytest
 
 from gallatin_gb300._abi import FAIL
 from oracle.oracle import (FIX_GATHER_EXIT_ROLLBACK, FIX_LEFTOVER_COMPLETES, PRODUCT_FIXES,
-                           Oracle, gen_leftover_trace)
+                           Oracle, gen_leftover_trace, gen_log_trace, gen_serial_trace)
 
 # (max_size, slice size of the largest class): one block per segment, and four
 GEOMETRIES = [(4096, 4096), (1024, 1024)]
@@ -42,3 +42,47 @@ def test_leftover_credit_returns_block_with_fix(max_size, slice_size):
     # whole segment released) than in the reference
     assert sv_fix.diff(sv_ref) != []
     assert PRODUCT_FIXES & FIX_LEFTOVER_COMPLETES
+
+
+# ---- trim: with nothing live, the trees, segment classes, slots and free
+# counters return to those of a fresh allocator (an addition of the product)
+
+TREE_FIELDS = ["seg_tree_words", "sub_tree_words", "tree_ids", "slots", "free_counters"]
+
+
+def free_everything(ops):
+    """The trace followed by a free of every allocation it leaves live."""
+    live = set()
+    for i, op in enumerate(ops):
+        if int(op) >> 63:
+            live.discard(int(op) & ~(1 << 63))
+        else:
+            live.add(i)
+    tail = np.array([(1 << 63) | i for i in sorted(live)], dtype=np.uint64)
+    return np.concatenate([np.asarray(ops, dtype=np.uint64), tail])
+
+
+@pytest.mark.parametrize("mk,nbytes", [
+    (lambda: gen_serial_trace(101, 20000, 55, 16, 256), 2 << 30),
+    (lambda: gen_log_trace(404, 4000, 55, 4, 26), 16 << 30),
+])
+def test_trim_after_freeing_everything_restores_fresh_trees(mk, nbytes):
+    o = Oracle(nbytes, 42)
+    fresh = o.export()
+    o.replay(free_everything(mk()))
+    assert o.export().diff(fresh, fields=TREE_FIELDS) != []  # pinned blocks still partly used
+    o.trim()
+    assert o.export().diff(fresh, fields=TREE_FIELDS) == []
+
+
+def test_trim_keeps_live_allocations_out_of_reach():
+    """A pinned block with live slices is retired, not reused: after trim the
+    slots hold other blocks, and freeing the live slices later completes it."""
+    ops = gen_serial_trace(7, 4096, 60, 16, 256)
+    o = Oracle(2 << 30, 42)
+    out = o.replay(ops)
+    live_blocks = {int(x) // 4096 for x, op in zip(out, ops) if not int(op) >> 63 and int(x) != FAIL}
+    before = o.export()
+    o.trim()
+    after = o.export()
+    assert not (set(after.slots.tolist()) & set(before.slots.tolist()) & live_blocks)
