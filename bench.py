@@ -258,12 +258,50 @@ def run_reference(args, world, rank):
     return line
 
 
+def run_tables(G):
+    """512 chained hash tables (2^12-2^22 pairs, seed 3), insert / delete 50% /
+    reinsert: batched and per-thread node allocation at the reference's
+    default knobs, the autotuner's sweep (batched form), and both forms at the
+    knobs it picks."""
+    from gallatin_gb300 import tables
+
+    def keep(d):
+        return {k: d[k] for k in ("ops_per_s", "ops", "op_ms", "violations", "nodes_allocated",
+                                  "deleted", "ms")}
+
+    sizes = tables.table_sizes(512, 12, 22, seed=3)
+    arena = 32 << 30
+    res = {"tables": 512, "pairs": int(sizes.sum())}
+    for form, batched in (("batched", True), ("plain", False)):
+        g = G.Gallatin.generate_on_device(arena, 42)
+        try:
+            res[form + "_default_knobs"] = keep(tables.run(g, sizes, 3, batched))
+        finally:
+            g.close()
+    t0 = time.time()
+    rows = tables.autotune(sizes, arena, batched=True)
+    res["autotune"] = {"points": len(rows), "seconds": time.time() - t0, "best": rows[0],
+                       "worst": rows[-1]}
+    best = rows[0]
+    knobs = dict(bytes_per_segment=best["segment_mib"] << 20, min_size=best["min_size"],
+                 max_size=best["max_size"], team_width=best["team_width"])
+    for form, batched in (("batched", True), ("plain", False)):
+        g = G.Gallatin.generate_on_device(arena, 42, **knobs)
+        try:
+            res[form + "_tuned_knobs"] = keep(tables.run(g, sizes, 3, batched))
+        finally:
+            g.close()
+    return res
+
+
 def run_configs(impl):
     """The secondary workloads, one JSON line.  Ours: the 1,048,576 x 16 B tid
     stamp on 2 GiB (the drop-in per-thread path) and the time of a 4,096-op
     serial trace replayed by one thread; large and block-size allocations on
-    64 GiB; the served request loop on 32 GiB.  --impl reference: the same
-    stamp through the reference build."""
+    64 GiB; the served request loop on 32 GiB; 512 chained hash tables with
+    the autotuner.  --impl reference: the same stamp through the reference
+    build (the reference's hash table has no delete and does not compile with
+    nvcc 13, so there is no reference run of the tables)."""
     import torch
     n, rounds = 1 << 20, 20
     out = {"metric": METRIC, "configs": True}
@@ -305,6 +343,7 @@ def run_configs(impl):
     out["large"] = large_block_workload(g)
     g.close()
     out["serve"] = serve.serve(400, arena_bytes=32 << 30, slots=32)
+    out["tables"] = run_tables(G)
     torch.cuda.synchronize()
     print(json.dumps(out))
 

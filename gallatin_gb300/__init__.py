@@ -50,6 +50,32 @@ class ChurnResult(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class TablesResult(C.Structure):
+    """gal_tables_result (gallatin_gb300/csrc/gal_tables.cu)."""
+    _fields_ = [
+        ("ms", C.c_float * 6),
+        ("total_pairs", C.c_uint64),
+        ("inserted", C.c_uint64),
+        ("deleted", C.c_uint64),
+        ("nodes_allocated", C.c_uint64),
+        ("nodes_freed", C.c_uint64),
+        ("spare_nodes_freed", C.c_uint64),
+        ("malloc_failed", C.c_uint64),
+        ("lock_timeouts", C.c_uint64),
+        ("missing", C.c_uint64),
+        ("unexpected", C.c_uint64),
+        ("wrong_value", C.c_uint64),
+        ("count_mismatch", C.c_uint64),
+        ("error_word", C.c_uint64),
+        ("setup_failed", C.c_uint64),
+    ]
+
+    def as_dict(self):
+        d = {f: getattr(self, f) for f, _ in self._fields_ if f != "ms"}
+        d["ms"] = [float(x) for x in self.ms]
+        return d
+
+
 def lib():
     """Load libgallatin_gb300.so (build it with gallatin_gb300.build.build())."""
     global _lib
@@ -97,6 +123,7 @@ def lib():
         "gal_bench_latency": ([vp, u64, u32, C.c_int, vp, vp], C.c_int),
         "gal_bench_atomic_peak": ([vp, vp], C.c_int),
         "gal_job_launch": ([vp, u32, u64, u64, vp, vp, vp], C.c_int),
+        "gal_bench_tables": ([vp, u32, vp, u64, C.c_int, vp, u32, vp, vp, u64, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -296,6 +323,23 @@ class Gallatin:
         _check(lib().gal_bench_latency(self._h, n, seed, int(batched), m.ctypes.data, f.ctypes.data),
                "gal_bench_latency")
         return m, f
+
+    def bench_tables(self, offsets, seed, batched, dump_table=None, dump_cap=0):
+        """The chained-hash-table workload (gal_tables.cu); offsets: uint64 prefix
+        sums of the table sizes.  Returns (TablesResult, dumped keys, values)."""
+        offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+        r = TablesResult()
+        keys = np.zeros(max(dump_cap, 1), dtype=np.uint64)
+        vals = np.zeros(max(dump_cap, 1), dtype=np.uint64)
+        n = np.zeros(1, dtype=np.uint64)
+        dump = dump_table is not None and dump_cap > 0
+        _check(lib().gal_bench_tables(self._h, len(offsets) - 1, offsets.ctypes.data, seed, int(batched),
+                                      C.byref(r), dump_table or 0,
+                                      keys.ctypes.data if dump else None,
+                                      vals.ctypes.data if dump else None, dump_cap,
+                                      n.ctypes.data if dump else None), "gal_bench_tables")
+        got = int(min(n[0], dump_cap)) if dump else 0
+        return r, keys[:got], vals[:got]
 
     def bench_stamp(self, n, size, rounds=1):
         ms = np.zeros(2, dtype=np.float32)

@@ -44,6 +44,7 @@ class GalConfig(C.Structure):
         ("zero_arena", C.c_uint32),
         ("spin_limit", C.c_uint32),
         ("gather_unlocked_below", C.c_uint32),
+        ("team_width", C.c_uint32),
     ]
 
 

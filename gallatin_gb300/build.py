@@ -15,7 +15,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgallatin_gb300.so")
-SOURCES = ["gal_lib.cu", "gal_bench.cu", "gal_noalloc.cu", "gal_serve.cu"]
+SOURCES = ["gal_lib.cu", "gal_bench.cu", "gal_noalloc.cu", "gal_serve.cu", "gal_tables.cu"]
 HEADERS = [
     os.path.join(ROOT, "include", "gallatin_gb300.h"),
     os.path.join(ROOT, "include", "gallatin_gb300", "gal_device.cuh"),

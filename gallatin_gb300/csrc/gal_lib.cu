@@ -269,6 +269,7 @@ int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot
     return GAL_ERR_ARGS;
   if (cfg.max_size < cfg.min_size || cfg.bytes_per_segment < cfg.max_size * 4096) return GAL_ERR_ARGS;
   if (cfg.subtree_policy > GAL_POLICY_LOWEST) return GAL_ERR_ARGS;
+  if (cfg.team_width > 32 || (cfg.team_width & (cfg.team_width - 1))) return GAL_ERR_ARGS;
   const uint32_t T = log2u(cfg.max_size) - log2u(cfg.min_size) + 1;
   const uint64_t S = num_bytes / cfg.bytes_per_segment;
   if (T > GAL_MAX_TREES || S == 0 || S + T + 1 >= 0xFFFF) return GAL_ERR_ARGS;
@@ -292,6 +293,7 @@ int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot
   st.smid_override = cfg.smid_override;
   st.spin_limit = cfg.spin_limit ? cfg.spin_limit : (1u << 16);
   st.gather_unlocked_below = cfg.gather_unlocked_below;
+  st.team_width = cfg.team_width ? cfg.team_width : 32;
   // pinned slots: first, halving per tree, floored (shared_block_storage.cuh:260-267);
   // pinned_slots_first == 0 asks for one slot per SM in every size class
   if (cfg.pinned_slots_first == 0) {
@@ -442,6 +444,7 @@ int gal_config_default(gal_config *cfg) {
   cfg->zero_arena = 1;
   cfg->spin_limit = 1u << 16;  // x backoff capped at 4 us: ~0.27 s per wait at most
   cfg->gather_unlocked_below = 0;
+  cfg->team_width = 32;
   return GAL_OK;
 }
 

@@ -66,6 +66,11 @@ typedef struct gal_config {
   uint32_t gather_unlocked_below; /* size classes with fewer blocks per segment
                                    gather segments without the class lock
                                    (0 = always lock, as gallatin.cuh:1538)       */
+  uint32_t team_width;          /* aggregation width of per-thread claims and
+                                   frees: lanes that share one atomic come from
+                                   aligned groups of this many (1..32, a power
+                                   of two; 32 or 0 = the whole warp, as the
+                                   reference's coalesced teams)                  */
 } gal_config;
 
 /* Aggregate statistics (stands in for Gallatin::print_info, gallatin.cuh:1855). */

@@ -75,6 +75,7 @@ struct state {
   uint32_t spin_limit;
   uint32_t total_slots;
   uint32_t gather_unlocked_below;  // see gal_config
+  uint32_t team_width;             // see gal_config (1..32, a power of two)
   uint32_t slot_base[GAL_MAX_TREES];
   uint32_t slot_count[GAL_MAX_TREES];
   veb_shape veb;
@@ -111,6 +112,13 @@ GAL_DEVICE_INLINE uint32_t lanemask_lt() {
   uint32_t r;
   asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(r));
   return r;
+}
+// The lanes this lane may aggregate with: the whole warp (team_width 32, the
+// reference's coalesced team) or its aligned group of team_width lanes.
+GAL_DEVICE_INLINE uint32_t team_group(const state *s) {
+  const uint32_t w = s->team_width;
+  if (w >= 32) return 0xFFFFFFFFu;
+  return ((1u << w) - 1u) << (lane_id() & ~(w - 1u));
 }
 GAL_DEVICE_INLINE uint32_t sm_id() {
   uint32_t r;
@@ -626,7 +634,7 @@ GAL_DEVICE_INLINE void credit_done(const state *s, uint32_t blk, uint32_t old, u
 // Gallatin::free_offset (gallatin.cuh:1774-1827): team by block, one atomic
 GAL_DEVICE_INLINE void free_block_slices(const state *s, uint32_t blk) {
   uint32_t active = active_lanes();
-  uint32_t team = __match_any_sync(active, blk);
+  uint32_t team = __match_any_sync(active, blk) & team_group(s);
   if ((int)lane_id() == __ffs(team) - 1) credit_frees(s, blk, (uint32_t)__popc(team));
 }
 
@@ -692,7 +700,7 @@ GAL_DEVICE_INLINE void *malloc_slices(const state *s, uint32_t tree, uint32_t co
   const uint64_t tid = thread_linear_id();
   for (int attempt = 0; attempt < SLICE_ATTEMPTS; attempt++) {
     const uint32_t active = active_lanes();
-    const uint32_t team = __match_any_sync(active, tree);
+    const uint32_t team = __match_any_sync(active, tree) & team_group(s);
     const int leader = __ffs(team) - 1;
     const int last = 31 - __clz(team);
     const uint32_t lt = lanemask_lt();
@@ -875,7 +883,7 @@ GAL_DEVICE_INLINE void free_n(const state *s, void *const (&p)[N], const bool (&
   for (int k = 0; k < N; k++) {
     if (blk[k] == NOBLK) continue;
     const uint32_t active = active_lanes();
-    const uint32_t team = __match_any_sync(active, blk[k]);
+    const uint32_t team = __match_any_sync(active, blk[k]) & team_group(s);
     lead[k] = (int)lane_id() == __ffs(team) - 1;
     cnt[k] = (uint32_t)__popc(team);
     if (lead[k]) old[k] = atomicAdd(&s->fctr[blk[k]], cnt[k]);

@@ -48,6 +48,7 @@ def test_default_config_is_reference_geometry(L):
     assert (cfg.bytes_per_segment, cfg.min_size, cfg.max_size) == (16 << 20, 16, 4096)
     assert (cfg.pinned_slots_first, cfg.pinned_slots_min) == (128, 4)
     assert cfg.smid_override == -1 and cfg.subtree_policy == G.GAL_POLICY_REFERENCE
+    assert cfg.team_width == 32
 
 
 @pytest.mark.parametrize("kw", [
@@ -56,6 +57,8 @@ def test_default_config_is_reference_geometry(L):
     dict(max_size=8192),                       # segment < max * 4096 (gallatin.cuh:300)
     dict(max_size=8),                          # max < min
     dict(subtree_policy=7),
+    dict(team_width=12),                       # not a power of two
+    dict(team_width=64),                       # wider than a warp
 ])
 def test_invalid_config_rejected_before_device_use(L, kw):
     import gallatin_gb300 as G
