@@ -24,6 +24,7 @@ GAL_DEV_ERR_BOOT = 0x40
 
 GAL_POLICY_REFERENCE = 0
 GAL_POLICY_LOWEST = 1
+GAL_ARENA_DEVICE, GAL_ARENA_HOST, GAL_ARENA_MANAGED = 0, 1, 2
 
 GAL_MAX_TREES = 16
 GAL_MAX_VEB_LAYERS = 8
@@ -45,6 +46,7 @@ class GalConfig(C.Structure):
         ("spin_limit", C.c_uint32),
         ("gather_unlocked_below", C.c_uint32),
         ("team_width", C.c_uint32),
+        ("arena_kind", C.c_uint32),
     ]
 
 

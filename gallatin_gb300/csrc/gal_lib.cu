@@ -32,6 +32,7 @@ namespace {
 std::mutex g_mu;
 std::unordered_map<const void *, gal_handle *> g_by_state;
 gal_handle *g_global = nullptr;
+gal_handle *g_global_host = nullptr;  // gal_init_host
 
 #define CUDA_TRY(x)                                                                   \
   do {                                                                                \
@@ -253,8 +254,30 @@ int persistent_grid(int device, K kernel) {
 void free_handle(gal_handle *h) {
   if (!h) return;
   if (h->meta) cudaFree(h->meta);
-  if (h->arena) cudaFree(h->arena);
+  if (h->arena) {
+    if (h->cfg.arena_kind == GAL_ARENA_HOST) cudaFreeHost(h->arena);
+    else cudaFree(h->arena);  // device and managed arenas
+  }
   delete h;
+}
+
+// the arena: device memory, pinned host memory mapped for the device (with
+// unified addressing its device address is the host address), or managed
+cudaError_t alloc_arena(gal_handle *h) {
+  switch (h->cfg.arena_kind) {
+    case GAL_ARENA_HOST: {
+      cudaError_t e = cudaHostAlloc((void **)&h->arena, h->arena_bytes, cudaHostAllocMapped);
+      if (e != cudaSuccess) return e;
+      void *dp = nullptr;
+      e = cudaHostGetDevicePointer(&dp, h->arena, 0);
+      if (e == cudaSuccess && dp != (void *)h->arena) e = cudaErrorInvalidValue;
+      return e;
+    }
+    case GAL_ARENA_MANAGED:
+      return cudaMallocManaged((void **)&h->arena, h->arena_bytes, cudaMemAttachGlobal);
+    default:
+      return cudaMalloc((void **)&h->arena, h->arena_bytes);
+  }
 }
 
 int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot, gal_handle **out) {
@@ -270,6 +293,7 @@ int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot
   if (cfg.max_size < cfg.min_size || cfg.bytes_per_segment < cfg.max_size * 4096) return GAL_ERR_ARGS;
   if (cfg.subtree_policy > GAL_POLICY_LOWEST) return GAL_ERR_ARGS;
   if (cfg.team_width > 32 || (cfg.team_width & (cfg.team_width - 1))) return GAL_ERR_ARGS;
+  if (cfg.arena_kind > GAL_ARENA_MANAGED) return GAL_ERR_ARGS;
   const uint32_t T = log2u(cfg.max_size) - log2u(cfg.min_size) + 1;
   const uint64_t S = num_bytes / cfg.bytes_per_segment;
   if (T > GAL_MAX_TREES || S == 0 || S + T + 1 >= 0xFFFF) return GAL_ERR_ARGS;
@@ -352,7 +376,7 @@ int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot
     return GAL_ERR_OOM;
   }
   h->arena_bytes = S * cfg.bytes_per_segment;
-  if (cudaMalloc(&h->arena, h->arena_bytes) != cudaSuccess) {
+  if (alloc_arena(h) != cudaSuccess) {
     cudaGetLastError();
     free_handle(h);
     return GAL_ERR_OOM;
@@ -445,6 +469,7 @@ int gal_config_default(gal_config *cfg) {
   cfg->spin_limit = 1u << 16;  // x backoff capped at 4 us: ~0.27 s per wait at most
   cfg->gather_unlocked_below = 0;
   cfg->team_width = 32;
+  cfg->arena_kind = GAL_ARENA_DEVICE;
   return GAL_OK;
 }
 
@@ -463,6 +488,7 @@ int gal_destroy(gal_handle *h) {
     std::lock_guard<std::mutex> g(g_mu);
     g_by_state.erase(h->d_state);
     if (g_global == h) g_global = nullptr;
+    if (g_global_host == h) g_global_host = nullptr;
   }
   free_handle(h);
   return GAL_OK;
@@ -631,6 +657,38 @@ int gal_teardown(void) {
 gal_handle *gal_global(void) {
   std::lock_guard<std::mutex> g(g_mu);
   return g_global;
+}
+
+int gal_init_host(uint64_t num_bytes, uint64_t seed, const gal_config *cfg) {
+  {
+    std::lock_guard<std::mutex> g(g_mu);
+    if (g_global_host) return GAL_ERR_STATE;
+  }
+  gal_config c;
+  if (cfg) c = *cfg;
+  else gal_config_default(&c);
+  c.arena_kind = GAL_ARENA_HOST;
+  gal_handle *h = nullptr;
+  int rc = gal_create(num_bytes, seed, &c, &h);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> g(g_mu);
+  g_global_host = h;
+  return GAL_OK;
+}
+
+int gal_teardown_host(void) {
+  gal_handle *h;
+  {
+    std::lock_guard<std::mutex> g(g_mu);
+    h = g_global_host;
+  }
+  if (!h) return GAL_ERR_STATE;
+  return gal_destroy(h);
+}
+
+gal_handle *gal_global_host(void) {
+  std::lock_guard<std::mutex> g(g_mu);
+  return g_global_host;
 }
 
 int gal_replay_trace(gal_handle *h, const uint64_t *ops, uint64_t nops, uint64_t *out_offsets,

@@ -19,8 +19,8 @@ namespace gallatin {
 namespace allocators {
 
 namespace detail {
-constexpr bool is_pow2(uint64_t x) { return x && !(x & (x - 1)); }
-constexpr int log2_exact(uint64_t x) { return x <= 1 ? 0 : 1 + log2_exact(x >> 1); }
+__host__ __device__ constexpr bool is_pow2(uint64_t x) { return x && !(x & (x - 1)); }
+__host__ __device__ constexpr int log2_exact(uint64_t x) { return x <= 1 ? 0 : 1 + log2_exact(x >> 1); }
 }  // namespace detail
 
 template <uint64_t bytes_per_segment, uint64_t smallest, uint64_t biggest>
@@ -45,11 +45,30 @@ struct Gallatin {
   // gallatin.cuh:324.  Returns nullptr (and prints why) if construction fails.
   static __host__ my_type *generate_on_device(uint64_t max_bytes, uint64_t seed, bool print_info = true,
                                               bool running_calloc = false) {
+    return generate_with_arena(max_bytes, seed, print_info, running_calloc, GAL_ARENA_DEVICE);
+  }
+
+  // gallatin.cuh:427: the arena in pinned host memory mapped into the device's
+  // address space; the allocator's metadata stays in device memory
+  static __host__ my_type *generate_on_device_host(uint64_t max_bytes, uint64_t seed, bool print_info = true,
+                                                   bool running_calloc = false) {
+    return generate_with_arena(max_bytes, seed, print_info, running_calloc, GAL_ARENA_HOST);
+  }
+
+  // gallatin.cuh:531: the arena in managed memory
+  static __host__ my_type *generate_on_device_managed(uint64_t max_bytes, uint64_t seed,
+                                                      bool print_info = true, bool running_calloc = false) {
+    return generate_with_arena(max_bytes, seed, print_info, running_calloc, GAL_ARENA_MANAGED);
+  }
+
+  static __host__ my_type *generate_with_arena(uint64_t max_bytes, uint64_t seed, bool print_info,
+                                               bool running_calloc, uint32_t arena_kind) {
     if (running_calloc) {
       fprintf(stderr, "Gallatin: calloc mode (dynamic parallelism) is not provided\n");
       return nullptr;
     }
     gal_config cfg = config();
+    cfg.arena_kind = arena_kind;
     gal_handle *h = nullptr;
     int rc = gal_create(max_bytes, seed, &cfg, &h);
     if (rc != GAL_OK) {

@@ -71,7 +71,17 @@ typedef struct gal_config {
                                    aligned groups of this many (1..32, a power
                                    of two; 32 or 0 = the whole warp, as the
                                    reference's coalesced teams)                  */
+  uint32_t arena_kind;          /* GAL_ARENA_*: where the arena lives; metadata
+                                   is always device memory                       */
 } gal_config;
+
+/* Arena backing (gal_config.arena_kind). */
+#define GAL_ARENA_DEVICE 0u  /* cudaMalloc (generate_on_device, gallatin.cuh:324)  */
+#define GAL_ARENA_HOST 1u    /* pinned host memory mapped into the device's
+                                address space (generate_on_device_host,
+                                gallatin.cuh:427)                                  */
+#define GAL_ARENA_MANAGED 2u /* cudaMallocManaged (generate_on_device_managed,
+                                gallatin.cuh:531)                                  */
 
 /* Aggregate statistics (stands in for Gallatin::print_info, gallatin.cuh:1855). */
 typedef struct gal_stats {
@@ -193,6 +203,12 @@ int gal_init(uint64_t num_bytes, uint64_t seed, const gal_config *cfg);
 int gal_teardown(void);
 /* The global handle (NULL before gal_init). */
 gal_handle *gal_global(void);
+/* The second process-global instance, with its arena in host memory: replaces
+ * init_global_allocator_host / free_global_allocator_host
+ * (global_allocator.cuh:100-123); cfg->arena_kind is forced to GAL_ARENA_HOST. */
+int gal_init_host(uint64_t num_bytes, uint64_t seed, const gal_config *cfg);
+int gal_teardown_host(void);
+gal_handle *gal_global_host(void);
 
 /* ---- device work launched by the library ---------------------------------- */
 

@@ -113,3 +113,199 @@ extern "C" int dropin_handle_test(uint64_t num_bytes, uint64_t n, uint64_t size,
   out[3] = err;
   return e == cudaSuccess ? 0 : 1;
 }
+
+// ---- host-backed, managed, fused and poisoned allocations
+// (global_allocator.cuh:100-357, gallatin.cuh:427-630)
+
+__global__ void host_malloc_stamp(uint64_t n, uint64_t size, uint64_t **bits, unsigned long long *c) {
+  uint64_t tid = threadIdx.x + (uint64_t)blockIdx.x * blockDim.x;
+  if (tid >= n) return;
+  uint64_t *p = (uint64_t *)global_malloc_host(size);
+  bits[tid] = p;
+  if (!p) {
+    atomicAdd(&c[0], 1ull);
+    return;
+  }
+  p[0] = tid;
+}
+
+__global__ void host_check_free(uint64_t n, uint64_t **bits, unsigned long long *c) {
+  uint64_t tid = threadIdx.x + (uint64_t)blockIdx.x * blockDim.x;
+  if (tid >= n) return;
+  uint64_t *p = bits[tid];
+  if (!p) return;
+  if (p[0] != tid) atomicAdd(&c[1], 1ull);
+  global_free_host(p);
+}
+
+// out[0] misses, [1] stamp errors seen on the device, [2] stamps the host read
+// wrong through the same pointers, [3] device error word
+extern "C" int dropin_host_test(uint64_t host_bytes, uint64_t n, uint64_t size, uint64_t *out) {
+  init_global_allocator_host(host_bytes, 42, false);
+  if (!gal_global_host()) return 2;
+  uint64_t **bits = nullptr;
+  unsigned long long *c = nullptr;
+  cudaMalloc(&bits, n * sizeof(uint64_t *));
+  cudaMalloc(&c, 4 * sizeof(unsigned long long));
+  cudaMemset(c, 0, 4 * sizeof(unsigned long long));
+  unsigned grid = (unsigned)((n + 255) / 256);
+  host_malloc_stamp<<<grid, 256>>>(n, size, bits, c);
+  cudaError_t e = cudaDeviceSynchronize();
+  // the allocations live in host memory: the host reads the stamps directly
+  uint64_t **hb = (uint64_t **)malloc(n * sizeof(uint64_t *));
+  cudaMemcpy(hb, bits, n * sizeof(uint64_t *), cudaMemcpyDeviceToHost);
+  uint64_t host_bad = 0;
+  for (uint64_t i = 0; i < n; i++)
+    if (hb[i] && hb[i][0] != i) host_bad++;
+  free(hb);
+  host_check_free<<<grid, 256>>>(n, bits, c);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  unsigned long long h[4] = {0, 0, 0, 0};
+  cudaMemcpy(h, c, sizeof(h), cudaMemcpyDeviceToHost);
+  uint32_t err = 0;
+  gal_last_error(gal_global_host(), &err);
+  print_global_stats_host();
+  cudaFree(bits);
+  cudaFree(c);
+  free_global_allocator_host();
+  out[0] = h[0];
+  out[1] = h[1];
+  out[2] = host_bad;
+  out[3] = err;
+  return e == cudaSuccess ? 0 : 1;
+}
+
+// managed arena through the handle API; out as dropin_host_test
+extern "C" int dropin_managed_test(uint64_t bytes, uint64_t n, uint64_t size, uint64_t *out) {
+  using gallatin_type = Gallatin<16ULL * 1024 * 1024, 16ULL, 4096ULL>;
+  gallatin_type *alloc = gallatin_type::generate_on_device_managed(bytes, 42, false);
+  if (!alloc) return 2;
+  uint64_t **bits = nullptr;
+  unsigned long long *c = nullptr;
+  cudaMalloc(&bits, n * sizeof(uint64_t *));
+  cudaMalloc(&c, 4 * sizeof(unsigned long long));
+  cudaMemset(c, 0, 4 * sizeof(unsigned long long));
+  unsigned grid = (unsigned)((n + 255) / 256);
+  handle_malloc<gallatin_type><<<grid, 256>>>(alloc, n, size, bits, c);
+  cudaError_t e = cudaDeviceSynchronize();
+  uint64_t **hb = (uint64_t **)malloc(n * sizeof(uint64_t *));
+  cudaMemcpy(hb, bits, n * sizeof(uint64_t *), cudaMemcpyDeviceToHost);
+  uint64_t host_bad = 0;
+  for (uint64_t i = 0; i < n; i++)
+    if (hb[i] && hb[i][0] != i) host_bad++;
+  free(hb);
+  handle_free<gallatin_type><<<grid, 256>>>(alloc, n, bits, c + 1);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  unsigned long long h[4] = {0, 0, 0, 0};
+  cudaMemcpy(h, c, sizeof(h), cudaMemcpyDeviceToHost);
+  uint32_t err = 0;
+  gal_last_error(gal_handle_of(alloc), &err);
+  cudaFree(bits);
+  cudaFree(c);
+  gallatin_type::free_on_device(alloc);
+  out[0] = h[0];
+  out[1] = h[1];
+  out[2] = host_bad + h[2];
+  out[3] = err;
+  return e == cudaSuccess ? 0 : 1;
+}
+
+__global__ void fused_malloc(uint64_t n, uint64_t size, uint64_t **bits, unsigned long long *c) {
+  uint64_t tid = threadIdx.x + (uint64_t)blockIdx.x * blockDim.x;
+  if (tid >= n) return;
+  uint64_t *p = (uint64_t *)global_malloc_fused(size);
+  bits[tid] = p;
+  if (!p) {
+    atomicAdd(&c[0], 1ull);
+    return;
+  }
+  if (!global_gallatin->owns_allocation(p)) atomicAdd(&c[2], 1ull);  // served from host memory
+  p[0] = tid;
+}
+
+__global__ void fused_free(uint64_t n, uint64_t **bits, unsigned long long *c) {
+  uint64_t tid = threadIdx.x + (uint64_t)blockIdx.x * blockDim.x;
+  if (tid >= n) return;
+  uint64_t *p = bits[tid];
+  if (!p) return;
+  if (p[0] != tid) atomicAdd(&c[1], 1ull);
+  global_free_fused(p);
+}
+
+// device arena too small for all requests: the rest come from host memory.
+// out[0] misses, [1] stamp errors, [2] served from host, [3] error words (OR)
+extern "C" int dropin_fused_test(uint64_t dev_bytes, uint64_t host_bytes, uint64_t n, uint64_t size,
+                                 uint64_t *out) {
+  init_global_allocator_combined(dev_bytes, host_bytes, 42, false);
+  if (!gal_global() || !gal_global_host()) return 2;
+  uint64_t **bits = nullptr;
+  unsigned long long *c = nullptr;
+  cudaMalloc(&bits, n * sizeof(uint64_t *));
+  cudaMalloc(&c, 4 * sizeof(unsigned long long));
+  cudaMemset(c, 0, 4 * sizeof(unsigned long long));
+  unsigned grid = (unsigned)((n + 255) / 256);
+  fused_malloc<<<grid, 256>>>(n, size, bits, c);
+  fused_free<<<grid, 256>>>(n, bits, c);
+  cudaError_t e = cudaDeviceSynchronize();
+  unsigned long long h[4] = {0, 0, 0, 0};
+  cudaMemcpy(h, c, sizeof(h), cudaMemcpyDeviceToHost);
+  uint32_t err = 0, err2 = 0;
+  gal_last_error(gal_global(), &err);
+  gal_last_error(gal_global_host(), &err2);
+  print_global_stats_combined();
+  cudaFree(bits);
+  cudaFree(c);
+  free_global_allocator_combined();
+  out[0] = h[0];
+  out[1] = h[1];
+  out[2] = h[2];
+  out[3] = err | err2;
+  return e == cudaSuccess ? 0 : 1;
+}
+
+// c[0] poisoned allocations failed, c[1] intact ones reported violated,
+// c[2] padding changes not reported, c[3] user-region checks failed
+__global__ void poison_roundtrip(uint64_t n, uint64_t bytes, unsigned long long *c) {
+  uint64_t tid = threadIdx.x + (uint64_t)blockIdx.x * blockDim.x;
+  if (tid >= n) return;
+  char *p = (char *)global_malloc_poison(bytes);
+  if (!p) {
+    atomicAdd(&c[0], 1ull);
+    return;
+  }
+  for (uint64_t i = 0; i < bytes; i++) p[i] = (char)(tid + i);  // the user region only
+  if (!global_check_poison(p)) atomicAdd(&c[1], 1ull);
+  // one byte past the user region: inside the allocation's padding
+  const uint64_t extra = global_gallatin->get_allocated_size(bytes + 32) - (bytes + 32);
+  if (extra > 0) {
+    char keep = p[bytes];
+    p[bytes] = (char)(keep ^ 0x5A);
+    if (global_check_poison(p)) atomicAdd(&c[2], 1ull);
+    p[bytes] = keep;
+  }
+  for (uint64_t i = 0; i < bytes; i++)
+    if (p[i] != (char)(tid + i)) {
+      atomicAdd(&c[3], 1ull);
+      break;
+    }
+  global_free_poison(p);
+}
+
+// out[0..3] as above, out[4] device error word
+extern "C" int dropin_poison_test(uint64_t num_bytes, uint64_t n, uint64_t bytes, uint64_t *out) {
+  init_global_allocator(num_bytes, 42, false);
+  unsigned long long *c = nullptr;
+  cudaMalloc(&c, 4 * sizeof(unsigned long long));
+  cudaMemset(c, 0, 4 * sizeof(unsigned long long));
+  poison_roundtrip<<<(unsigned)((n + 255) / 256), 256>>>(n, bytes, c);
+  cudaError_t e = cudaDeviceSynchronize();
+  unsigned long long h[4] = {0, 0, 0, 0};
+  cudaMemcpy(h, c, sizeof(h), cudaMemcpyDeviceToHost);
+  uint32_t err = 0;
+  gal_last_error(gal_global(), &err);
+  cudaFree(c);
+  free_global_allocator();
+  for (int i = 0; i < 4; i++) out[i] = h[i];
+  out[4] = err;
+  return e == cudaSuccess ? 0 : 1;
+}

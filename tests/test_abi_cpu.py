@@ -59,6 +59,7 @@ def test_default_config_is_reference_geometry(L):
     dict(subtree_policy=7),
     dict(team_width=12),                       # not a power of two
     dict(team_width=64),                       # wider than a warp
+    dict(arena_kind=3),                        # device, host or managed only
 ])
 def test_invalid_config_rejected_before_device_use(L, kw):
     import gallatin_gb300 as G

@@ -39,3 +39,47 @@ def test_handle_api_tid_stamp(D):
     out = np.zeros(4, dtype=np.uint64)
     assert D.dropin_handle_test(2 << 30, 1 << 20, 16, 3, out.ctypes.data) == 0
     assert out.tolist() == [0, 0, 0, 0]
+
+
+def _fn(D, name, nargs):
+    f = getattr(D, name)
+    f.argtypes = [C.c_uint64] * nargs + [C.c_void_p]
+    f.restype = C.c_int
+    return f
+
+
+def test_host_backed_global_instance(D):
+    """init_global_allocator_host / global_malloc_host / global_free_host: the
+    allocations live in pinned host memory; the host reads the device's stamps
+    through the same pointers."""
+    out = np.zeros(4, dtype=np.uint64)
+    assert _fn(D, "dropin_host_test", 3)(256 << 20, 1 << 16, 64, out.ctypes.data) == 0
+    assert out.tolist() == [0, 0, 0, 0]
+
+
+def test_managed_arena_handle(D):
+    """Gallatin<...>::generate_on_device_managed: the same tid stamps, read on
+    the host through managed memory."""
+    out = np.zeros(4, dtype=np.uint64)
+    assert _fn(D, "dropin_managed_test", 3)(1 << 30, 1 << 16, 64, out.ctypes.data) == 0
+    assert out.tolist() == [0, 0, 0, 0]
+
+
+def test_fused_malloc_falls_back_to_host(D):
+    """global_malloc_fused: a 512 MiB device arena cannot hold 1 GiB of 4 KiB
+    requests, so part of them is served from the host instance; every stamp
+    survives and global_free_fused returns each pointer to its owner."""
+    out = np.zeros(4, dtype=np.uint64)
+    assert _fn(D, "dropin_fused_test", 4)(512 << 20, 2 << 30, 1 << 18, 4096, out.ctypes.data) == 0
+    misses, bad, on_host, err = out.tolist()
+    assert misses == 0 and bad == 0 and err == 0
+    assert 0 < on_host < 1 << 18
+
+
+def test_poison_detects_padding_writes(D):
+    """global_malloc_poison / global_check_poison / global_free_poison: intact
+    allocations pass, a byte changed in the padding after the user region is
+    reported, the user region is untouched."""
+    out = np.zeros(5, dtype=np.uint64)
+    assert _fn(D, "dropin_poison_test", 3)(2 << 30, 1 << 14, 100, out.ctypes.data) == 0
+    assert out.tolist() == [0, 0, 0, 0, 0]
