@@ -64,6 +64,8 @@ def parse():
     p.add_argument("--unlocked", type=int, default=16,
                    help="batched form: classes with fewer blocks per segment gather without the lock")
     p.add_argument("--segment-mib", type=int, default=64, help="batched form: segment size")
+    p.add_argument("--spares", type=int, default=1, choices=[0, 1],
+                   help="batched form: a service warp keeps every pinned slot's next block prepared")
     p.add_argument("--min-size", type=int, default=16, help="batched form: smallest slice")
     p.add_argument("--max-size", type=int, default=4096, help="batched form: largest slice")
     p.add_argument("--free-mode", default="warp", choices=["cta", "warp"],
@@ -372,7 +374,7 @@ def main():
     # the reference's defaults (128 pinned slots halving to 4)
     tuned = dict(pinned_slots_first=args.slots, pinned_slots_min=args.slots if args.slots else 0,
                  gather_unlocked_below=args.unlocked, bytes_per_segment=args.segment_mib << 20,
-                 min_size=args.min_size, max_size=args.max_size)
+                 min_size=args.min_size, max_size=args.max_size, spare_blocks=args.spares)
     g = G.Gallatin.generate_on_device(arena, ALLOC_SEED, **tuned)
 
     # one probe step: a workload that does not fit would run the out-of-memory
@@ -470,6 +472,7 @@ def main():
         "config": {"workload": WORKLOAD, "path": "batched: CTA-aggregated persistent kernels, one CUDA graph per step",
                    "pinned_slots_batched": args.slots or "one per SM", "pinned_slots_plain": "128 halving to 4",
                    "batched_knobs": {"gather_unlocked_below": args.unlocked, "segment_mib": args.segment_mib,
+                                     "spare_blocks": args.spares,
                                      "min_size": args.min_size, "max_size": args.max_size,
                                      "free_mode": args.free_mode},
                    "arena_bytes": arena, "threads_per_round": N, "rounds": R,

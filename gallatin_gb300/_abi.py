@@ -47,6 +47,7 @@ class GalConfig(C.Structure):
         ("gather_unlocked_below", C.c_uint32),
         ("team_width", C.c_uint32),
         ("arena_kind", C.c_uint32),
+        ("spare_blocks", C.c_uint32),
     ]
 
 

@@ -10,6 +10,8 @@ ranks them by malloc+free ops/s:
   pinned slots       {one per SM, 128 halving to 4}   (block-buffer breadth)
   gather_unlocked_below {0, 16}            (classes that gather without a lock)
   free aggregation   {warp team, CTA}      (aggregation width of frees)
+  spare blocks       {off, on}             (block-buffer depth: a prepared next
+                                            block per pinned slot)
 
 Combinations the reference rejects (bytes_per_segment < max_size * 4096,
 gallatin.cuh:300) are skipped, so 4 MiB segments drop out for max 4096.
@@ -26,19 +28,19 @@ ARENA = 128 << 30
 
 
 def grid():
-    for seg, mn, mx, slots, unlocked, free_mode in itertools.product(
-            (16, 64), (16, 128), (4096, 16384), (0, 128), (0, 16), ("warp", "cta")):
+    for seg, mn, mx, slots, unlocked, free_mode, spares in itertools.product(
+            (16, 64), (16, 128), (4096, 16384), (0, 128), (0, 16), ("warp", "cta"), (0, 1)):
         if (seg << 20) < mx * 4096:
             continue
         yield dict(segment_mib=seg, min_size=mn, max_size=mx, slots=slots, unlocked=unlocked,
-                   free_mode=free_mode)
+                   free_mode=free_mode, spares=spares)
 
 
 def run_one(G, knobs, n, rounds, steps, seed=1):
     cfg = dict(bytes_per_segment=knobs["segment_mib"] << 20, min_size=knobs["min_size"],
                max_size=knobs["max_size"], pinned_slots_first=knobs["slots"],
                pinned_slots_min=knobs["slots"] if knobs["slots"] else 0,
-               gather_unlocked_below=knobs["unlocked"])
+               gather_unlocked_below=knobs["unlocked"], spare_blocks=knobs.get("spares", 0))
     if knobs["slots"] == 128:
         cfg["pinned_slots_min"] = 4
     g = G.Gallatin.generate_on_device(ARENA, 42, **cfg)

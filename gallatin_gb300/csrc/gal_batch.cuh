@@ -7,7 +7,11 @@
 // hash so each touched block gets one free-counter atomic per CTA.
 //
 // Both entry points must be reached by every thread of the CTA (they contain
-// __syncthreads); threads without work pass has_request = false / ptr = nullptr.
+// CTA barriers; with a service warp, by every worker thread: see
+// cta_claim_init); threads without work pass has_request = false / ptr = nullptr.
+// With gal_config.spare_blocks, a service warp keeps the next block of each
+// pinned slot the CTA uses prepared, so a claim that exhausts its block swaps
+// the spare in instead of searching the class's segments itself.
 // Requests that the aggregated path cannot serve (whole blocks, segment runs,
 // multi-slice sizes, or a claim that ran out of attempts) fall back to the
 // per-thread gal::malloc / gal::free of gal_device.cuh.
@@ -23,6 +27,9 @@ static constexpr int CTA_CLAIM_ATTEMPTS = 64;
 struct cta_claim_smem {
   uint32_t cached[GAL_MAX_TREES];       // block a persistent CTA last claimed from, per class
   uint32_t cached_slot[GAL_MAX_TREES];
+  uint32_t refill[GAL_MAX_TREES];       // slot whose spare the service warp should prepare
+  uint32_t workers;                     // threads that call cta_malloc (the rest: service warp)
+  uint32_t stop;                        // set once the workers are done
   uint32_t count[GAL_MAX_TREES];
   uint32_t nruns[GAL_MAX_TREES];
   uint32_t run_blk[GAL_MAX_TREES][CTA_RUNS];
@@ -69,7 +76,15 @@ static __device__ __noinline__ void cta_claim_class(const state *s, uint32_t tre
       blk = NOBLK;
     }
     if (crossed) {
-      replace_block(s, tree, slot, used, tid);
+      const uint32_t si = s->slot_base[tree] + slot;
+      uint32_t nx = NOBLK;
+      if (s->use_spares && sm.workers != blockDim.x) nx = atomicExch(s->spares + si, NOBLK);
+      if (nx != NOBLK) {  // the prepared block: one swap
+        if (atomicCAS(s->slots + si, used, nx) != used) credit_frees(s, nx, SLICES_PER_BLOCK);
+      } else {
+        replace_block(s, tree, slot, used, tid);
+      }
+      if (s->use_spares && sm.workers != blockDim.x) atomicExch(&sm.refill[tree], si);
       blk = NOBLK;
     }
   }
@@ -78,52 +93,124 @@ static __device__ __noinline__ void cta_claim_class(const state *s, uint32_t tre
   sm.cached_slot[tree] = slot;
 }
 
-// Call once at the start of a kernel that uses cta_malloc, before its loop.
-__device__ __forceinline__ void cta_claim_init(cta_claim_smem &sm) {
+// Call once at the start of a kernel that uses cta_malloc, before its loop,
+// followed by a __syncthreads().  workers: how many threads (a multiple of 32,
+// from thread 0) call cta_malloc; the last warp beyond them, if any, runs
+// cta_service.  0 = every thread of the CTA calls cta_malloc.
+__device__ __forceinline__ void cta_claim_init(cta_claim_smem &sm, uint32_t workers = 0) {
   if (threadIdx.x < GAL_MAX_TREES) {
     sm.cached[threadIdx.x] = NOBLK;
     sm.cached_slot[threadIdx.x] = 0;
+    sm.refill[threadIdx.x] = NOBLK;
   }
+  if (threadIdx.x == 0) {
+    sm.workers = workers ? workers : blockDim.x;
+    sm.stop = 0;
+  }
+}
+
+// barrier of the threads that call cta_malloc (named barrier 1 when a service
+// warp runs beside them, which never joins it)
+__device__ __forceinline__ void cta_sync(const cta_claim_smem &sm) {
+  const uint32_t w = *(const volatile uint32_t *)&sm.workers;
+  if (w == blockDim.x) {
+    __syncthreads();
+  } else {
+    asm volatile("bar.sync 1, %0;" ::"r"(w) : "memory");
+  }
+}
+
+// The service warp of a CTA-aggregated kernel: prepares the spare block of a
+// slot whose block a claim of this CTA just replaced, off the claims' path.
+// Returns when the workers set `stop` (or after a bounded number of polls).
+GAL_DEVICE_COLD void cta_service(const state *s, cta_claim_smem &sm) {
+  if (lane_id() != 0 || !s->use_spares) return;
+  const uint64_t tid = thread_linear_id();
+  for (uint32_t it = 0; it < (1u << 24); it++) {
+    bool work = false;
+    for (uint32_t t = 0; t < s->num_trees; t++) {
+      const uint32_t si = atomicExch(&sm.refill[t], NOBLK);
+      if (si == NOBLK) continue;
+      work = true;
+      if (ld_rlx(s->spares + si) != NOBLK) continue;
+      const uint32_t nb = request_block(s, t, tid);
+      if (nb == NOBLK) continue;
+      __threadfence();
+      if (atomicCAS(s->spares + si, NOBLK, nb) != NOBLK) credit_frees(s, nb, SLICES_PER_BLOCK);
+    }
+    if (*(volatile uint32_t *)&sm.stop) return;
+    if (!work) __nanosleep(256);
+  }
+}
+
+// The workers' last call: after it the service warp returns.
+__device__ __forceinline__ void cta_workers_done(cta_claim_smem &sm) {
+  cta_sync(sm);
+  if (threadIdx.x == 0) *(volatile uint32_t *)&sm.stop = 1u;
+}
+
+// Serves K requests per thread (request k of every thread of the CTA ranked
+// together, one claim per class for all of them); out[k] = nullptr where
+// has_request[k] is false.  More requests per call amortise the claim round
+// trip and the CTA barriers over more allocations.
+template <int K>
+__device__ __forceinline__ void cta_malloc_n(const state *s, const uint64_t (&size)[K],
+                                             const bool (&has_request)[K], cta_claim_smem &sm,
+                                             void *(&out)[K]) {
+  const uint32_t T = s->num_trees;
+  if (threadIdx.x < GAL_MAX_TREES) sm.count[threadIdx.x] = 0;
+  cta_sync(sm);
+  int tree[K];
+  uint32_t rank[K];
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    tree[k] = -1;
+    rank[k] = 0;
+    if (has_request[k]) {
+      int bits = ceil_log2(size[k]);
+      int t = (size[k] >> s->min_shift) == 0 ? 0 : bits - (int)s->min_shift;
+      if (t < (int)T) {
+        tree[k] = t;
+        rank[k] = atomicAdd(&sm.count[t], 1u);
+      }
+    }
+  }
+  cta_sync(sm);
+  if (threadIdx.x < T && sm.count[threadIdx.x] > 0)
+    cta_claim_class(s, threadIdx.x, sm.count[threadIdx.x], sm);
+  cta_sync(sm);
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    void *p = nullptr;
+    bool fallback = has_request[k] && tree[k] < 0;
+    if (tree[k] >= 0) {
+      const int t = tree[k];
+      uint32_t r = rank[k];
+      fallback = true;
+      for (uint32_t j = 0; j < sm.nruns[t]; j++) {
+        uint32_t len = sm.run_len[t][j];
+        if (r < len) {
+          p = slice_ptr(s, sm.run_blk[t][j], sm.run_start[t][j] + r, (uint32_t)t);
+          fallback = false;
+          break;
+        }
+        r -= len;
+      }
+    }
+    if (fallback) p = gal::malloc(s, size[k]);
+    out[k] = p;
+  }
+  cta_sync(sm);
 }
 
 // Returns this thread's allocation (nullptr when has_request is false).
 __device__ __forceinline__ void *cta_malloc(const state *s, uint64_t size, bool has_request,
                                             cta_claim_smem &sm) {
-  const uint32_t T = s->num_trees;
-  if (threadIdx.x < GAL_MAX_TREES) sm.count[threadIdx.x] = 0;
-  __syncthreads();
-  int tree = -1;
-  uint32_t rank = 0;
-  if (has_request) {
-    int bits = ceil_log2(size);
-    int t = (size >> s->min_shift) == 0 ? 0 : bits - (int)s->min_shift;
-    if (t < (int)T) {
-      tree = t;
-      rank = atomicAdd(&sm.count[t], 1u);
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x < T && sm.count[threadIdx.x] > 0)
-    cta_claim_class(s, threadIdx.x, sm.count[threadIdx.x], sm);
-  __syncthreads();
-  void *p = nullptr;
-  bool fallback = has_request && tree < 0;
-  if (tree >= 0) {
-    uint32_t r = rank;
-    fallback = true;
-    for (uint32_t k = 0; k < sm.nruns[tree]; k++) {
-      uint32_t len = sm.run_len[tree][k];
-      if (r < len) {
-        p = slice_ptr(s, sm.run_blk[tree][k], sm.run_start[tree][k] + r, (uint32_t)tree);
-        fallback = false;
-        break;
-      }
-      r -= len;
-    }
-  }
-  if (fallback) p = gal::malloc(s, size);
-  __syncthreads();
-  return p;
+  const uint64_t sz[1] = {size};
+  const bool has[1] = {has_request};
+  void *out[1];
+  cta_malloc_n<1>(s, sz, has, sm, out);
+  return out[0];
 }
 
 template <int SLOTS>

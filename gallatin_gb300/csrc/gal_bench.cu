@@ -70,26 +70,45 @@ __global__ void __launch_bounds__(FREE_BT)
   galwl::churn_free_warps(&a, ptrs, live, nslots, round, seed, all != 0, stats, lists[threadIdx.x >> 5]);
 }
 
-// persistent, CTA-aggregated malloc phase of one round
+// persistent, CTA-aggregated malloc phase of one round: BW worker threads and
+// one service warp (spare blocks) per CTA; each iteration of the workers serves
+// K x BW requests (request k of worker t is slot c + k*BW + t, so a warp's lanes
+// keep 32 consecutive slots for the liveness words)
+constexpr int BW = BT - 32;
+template <int K>
 __global__ void __launch_bounds__(BT)
     k_churn_malloc_batched(const gal::state *s, void **ptrs, uint32_t *live, uint64_t base,
                            uint64_t n, uint32_t seed, unsigned long long *stats) {
   __shared__ gal::cta_claim_smem sm;
-  gal::cta_claim_init(sm);
-  for (uint64_t c = (uint64_t)blockIdx.x * BT; c < n; c += (uint64_t)gridDim.x * BT) {
-    uint64_t t = c + threadIdx.x;
-    bool has = t < n;
-    uint64_t slot = base + t;
-    uint64_t size = has ? galwl::mixed_size(slot, seed) : 0;
-    void *p = gal::cta_malloc(s, size, has, sm);
-    if (has) {  // whole warps: n is a multiple of SLOT_ALIGN
-      if (p) *(volatile uint32_t *)p = galwl::payload(slot, seed);
-      ptrs[slot] = p;
-      galwl::publish_live(live, slot, p != nullptr);
-      galwl::warp_count(&stats[0], p != nullptr);
-      galwl::warp_count(&stats[1], p == nullptr);
+  gal::cta_claim_init(sm, BW);
+  __syncthreads();
+  if (threadIdx.x >= BW) {
+    gal::cta_service(s, sm);
+    return;
+  }
+  for (uint64_t c = (uint64_t)blockIdx.x * BW * K; c < n; c += (uint64_t)gridDim.x * BW * K) {
+    uint64_t size[K];
+    bool has[K];
+    void *p[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      const uint64_t t = c + (uint64_t)k * BW + threadIdx.x;
+      has[k] = t < n;  // whole warps: n is a multiple of SLOT_ALIGN
+      size[k] = has[k] ? galwl::mixed_size(base + t, seed) : 0;
+    }
+    gal::cta_malloc_n<K>(s, size, has, sm, p);
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      if (!has[k]) continue;
+      const uint64_t slot = base + c + (uint64_t)k * BW + threadIdx.x;
+      if (p[k]) *(volatile uint32_t *)p[k] = galwl::payload(slot, seed);
+      ptrs[slot] = p[k];
+      galwl::publish_live(live, slot, p[k] != nullptr);
+      galwl::warp_count(&stats[0], p[k] != nullptr);
+      galwl::warp_count(&stats[1], p[k] == nullptr);
     }
   }
+  gal::cta_workers_done(sm);
 }
 
 // persistent, CTA-aggregated free phase (coin flips, or everything when all)
@@ -206,8 +225,13 @@ __global__ void __launch_bounds__(BT)
     k_lat_malloc_batched(const gal::state *s, void **ptrs, uint64_t base, uint64_t n, uint32_t seed,
                          uint32_t *cycles) {
   __shared__ gal::cta_claim_smem sm;
-  gal::cta_claim_init(sm);
-  for (uint64_t c = (uint64_t)blockIdx.x * BT; c < n; c += (uint64_t)gridDim.x * BT) {
+  gal::cta_claim_init(sm, BW);
+  __syncthreads();
+  if (threadIdx.x >= BW) {
+    gal::cta_service(s, sm);
+    return;
+  }
+  for (uint64_t c = (uint64_t)blockIdx.x * BW; c < n; c += (uint64_t)gridDim.x * BW) {
     uint64_t t = c + threadIdx.x;
     bool has = t < n;
     uint64_t size = has ? galwl::mixed_size(base + t, seed) : 0;
@@ -220,6 +244,7 @@ __global__ void __launch_bounds__(BT)
       cycles[t] = (uint32_t)min(c1 - c0, 0xFFFFFFFFll);
     }
   }
+  gal::cta_workers_done(sm);
 }
 
 // the batched free path (gal_free_batched): warp teams per block through
@@ -264,7 +289,8 @@ struct churn_ctx {
   void **ptrs;
   uint32_t *live;  // slot liveness bits (churn.cuh)
   unsigned long long *stats;
-  int grid_b;  // persistent grids: batched malloc/free, warp free phase
+  int k_shift;  // batched malloc: 2^k_shift requests per thread per iteration
+  int grid_b;   // persistent grids: batched malloc/free, warp free phase
   int grid_f;
   std::vector<cudaEvent_t> ev;  // [2 per kernel]
   int nk = 0;
@@ -307,8 +333,15 @@ void enqueue_step(churn_ctx &c, cudaStream_t st, bool capturing) {
     uint64_t base = c.N * r;
     mark(0, true);
     if (c.batched & 1) {
-      unsigned g = (unsigned)std::min<uint64_t>((c.N + BT - 1) / BT, (uint64_t)c.grid_b);
-      k_churn_malloc_batched<<<g, BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats);
+      const int per = 1 << c.k_shift;  // requests per thread per iteration
+      unsigned gk = (unsigned)std::min<uint64_t>((c.N + (uint64_t)BW * per - 1) / ((uint64_t)BW * per),
+                                                 (uint64_t)c.grid_b);
+      if (c.k_shift == 2)
+        k_churn_malloc_batched<4><<<gk, BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats);
+      else if (c.k_shift == 1)
+        k_churn_malloc_batched<2><<<gk, BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats);
+      else
+        k_churn_malloc_batched<1><<<gk, BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats);
     } else {
       k_churn_malloc_plain<<<(unsigned)((c.N + 255) / 256), 256, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed,
                                                                         c.stats);
@@ -335,8 +368,10 @@ extern "C" {
 /* Mixed-size churn.  One step = `rounds` x (coin frees of the live slots before
  * every round but the first, then threads_per_round mallocs), then a drain of
  * all live slots; every step serves the same requests.  batched: bit 0 CTA-aggregated
- * malloc, bit 1 CTA-aggregated free (else per-thread with warp teams); CTA-aggregated
- * persistent kernels; use_graph: the step is one captured CUDA graph.
+ * malloc, bit 1 CTA-aggregated free (else per-thread with warp teams), bits 4-5:
+ * log2 of the requests each thread of the CTA-aggregated malloc serves per
+ * iteration (0-2); CTA-aggregated persistent kernels; use_graph: the step is one
+ * captured CUDA graph.
  * step_ms[i]: duration of timed step i (CUDA events on the launching stream). */
 int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, uint32_t seed,
                     int batched, int use_graph, int warmup, int steps, float *step_ms,
@@ -350,7 +385,9 @@ int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, 
   c.N = threads_per_round;
   c.R = rounds;
   c.seed = seed;
-  c.batched = batched;
+  c.batched = batched & 3;
+  c.k_shift = (batched >> 4) & 3;
+  if (c.k_shift > 2) return GAL_ERR_ARGS;
   c.ptrs = nullptr;
   c.live = nullptr;
   c.stats = nullptr;
@@ -363,7 +400,7 @@ int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, 
   memset(res, 0, sizeof(*res));
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_churn_malloc_batched, BT, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_churn_malloc_batched<1>, BT, 0);
   c.grid_b = sms * (per_sm > 0 ? per_sm : 1);
   per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_churn_free_plain, FREE_BT, 0);
@@ -570,7 +607,7 @@ int gal_bench_latency(gal_handle *h, uint64_t n, uint32_t seed, int batched,
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lat_malloc_batched, BT, 0);
-  unsigned gb = (unsigned)std::min<uint64_t>((n + BT - 1) / BT, (uint64_t)sms * (per_sm > 0 ? per_sm : 1));
+  unsigned gb = (unsigned)std::min<uint64_t>((n + BW - 1) / BW, (uint64_t)sms * (per_sm > 0 ? per_sm : 1));
   unsigned gp = (unsigned)((n + 255) / 256);
   CK(cudaMalloc(&ptrs, n * sizeof(void *)));
   CK(cudaMalloc(&cm, n * 4));

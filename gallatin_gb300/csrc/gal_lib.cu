@@ -78,6 +78,13 @@ __global__ void k_boot(const gal::state *s) {
 // boot the slots again in the one-thread order.
 __global__ void k_trim(const gal::state *s) {
   if (threadIdx.x + blockIdx.x * blockDim.x != 0) return;
+  for (uint32_t i = 0; i < s->total_slots; i++) {  // spare blocks: nothing handed out
+    uint32_t blk = atomicExch(s->spares + i, gal::NOBLK);
+    if (blk == gal::NOBLK) continue;
+    unsigned long long old = atomicAdd(&s->mwords[blk], (unsigned long long)gal::SLICES_PER_BLOCK);
+    uint32_t handed_out = (uint32_t)old;
+    if (handed_out < gal::SLICES_PER_BLOCK) gal::credit_frees(s, blk, gal::SLICES_PER_BLOCK - handed_out);
+  }
   for (uint32_t t = 0; t < s->num_trees; t++)
     for (uint32_t i = 0; i < s->slot_count[t]; i++) {
       uint32_t blk = atomicExch(s->slots + s->slot_base[t] + i, gal::NOBLK);
@@ -203,17 +210,27 @@ __global__ void k_free_per_thread(const gal::state *s, void *const *ptrs, uint64
 
 constexpr int BATCH_THREADS = 512;
 
+// BATCH_WORKERS threads claim; the CTA's last warp prepares spare blocks
+// (gal_config.spare_blocks) off the claims' path
+constexpr int BATCH_WORKERS = BATCH_THREADS - 32;
+
 __global__ void __launch_bounds__(BATCH_THREADS)
     k_malloc_batched(const gal::state *s, const uint64_t *sizes, uint64_t n, void **out) {
   __shared__ gal::cta_claim_smem sm;
-  gal::cta_claim_init(sm);
-  for (uint64_t base = (uint64_t)blockIdx.x * BATCH_THREADS; base < n;
-       base += (uint64_t)gridDim.x * BATCH_THREADS) {
+  gal::cta_claim_init(sm, BATCH_WORKERS);
+  __syncthreads();
+  if (threadIdx.x >= BATCH_WORKERS) {
+    gal::cta_service(s, sm);
+    return;
+  }
+  for (uint64_t base = (uint64_t)blockIdx.x * BATCH_WORKERS; base < n;
+       base += (uint64_t)gridDim.x * BATCH_WORKERS) {
     uint64_t i = base + threadIdx.x;
     bool has = i < n;
     void *p = gal::cta_malloc(s, has ? sizes[i] : 0, has, sm);
     if (has) out[i] = p;
   }
+  gal::cta_workers_done(sm);
 }
 
 // Batched free: each thread takes FREE_PER_THREAD consecutive entries per
@@ -294,6 +311,7 @@ int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot
   if (cfg.subtree_policy > GAL_POLICY_LOWEST) return GAL_ERR_ARGS;
   if (cfg.team_width > 32 || (cfg.team_width & (cfg.team_width - 1))) return GAL_ERR_ARGS;
   if (cfg.arena_kind > GAL_ARENA_MANAGED) return GAL_ERR_ARGS;
+  if (cfg.spare_blocks > 1) return GAL_ERR_ARGS;
   const uint32_t T = log2u(cfg.max_size) - log2u(cfg.min_size) + 1;
   const uint64_t S = num_bytes / cfg.bytes_per_segment;
   if (T > GAL_MAX_TREES || S == 0 || S + T + 1 >= 0xFFFF) return GAL_ERR_ARGS;
@@ -318,6 +336,7 @@ int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot
   st.spin_limit = cfg.spin_limit ? cfg.spin_limit : (1u << 16);
   st.gather_unlocked_below = cfg.gather_unlocked_below;
   st.team_width = cfg.team_width ? cfg.team_width : 32;
+  st.use_spares = cfg.spare_blocks ? 1u : 0u;
   // pinned slots: first, halving per tree, floored (shared_block_storage.cuh:260-267);
   // pinned_slots_first == 0 asks for one slot per SM in every size class
   if (cfg.pinned_slots_first == 0) {
@@ -369,6 +388,7 @@ int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot
   size_t o_act = carve(S * 4), o_qc = carve(S * 4), o_qfc = carve(S * 4), o_fqfc = carve(S * 4);
   size_t o_mw = carve(nblocks * 8), o_fc = carve(nblocks * 4), o_q = carve(nblocks * 4);
   size_t o_slots = carve(total * 4);
+  size_t o_spares = carve(total * 4);
   size_t o_locks = carve(128), o_err = carve(128);
   h->meta_bytes = off;
   if (cudaMalloc(&h->meta, h->meta_bytes) != cudaSuccess) {
@@ -394,6 +414,7 @@ int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot
   st.fctr = (uint32_t *)(m + o_fc);
   st.queues = (uint32_t *)(m + o_q);
   st.slots = (uint32_t *)(m + o_slots);
+  st.spares = (uint32_t *)(m + o_spares);
   st.locks = (uint32_t *)(m + o_locks);
   st.error = (uint32_t *)(m + o_err);
   h->d_state = (gal::state *)(m + o_state);
@@ -406,6 +427,7 @@ int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot
     if (cudaMemset(st.active, 0xFF, S * 4) != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
     if (cudaMemset(st.queues, 0xFF, nblocks * 4) != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
     if (cudaMemset(st.slots, 0xFF, total * 4) != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
+    if (cudaMemset(st.spares, 0xFF, total * 4) != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
     k_init_words<<<1024, 256>>>(st.mwords, nblocks, st.seg_tree, st.veb);
     if (cudaGetLastError() != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
     if (cfg.zero_arena && cudaMemset(h->arena, 0, h->arena_bytes) != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
@@ -470,6 +492,7 @@ int gal_config_default(gal_config *cfg) {
   cfg->gather_unlocked_below = 0;
   cfg->team_width = 32;
   cfg->arena_kind = GAL_ARENA_DEVICE;
+  cfg->spare_blocks = 0;
   return GAL_OK;
 }
 
@@ -603,6 +626,7 @@ int gal_import_state(gal_handle *h, const gal_state_view *v) {
   CUDA_TRY(cudaMemcpy(st.fctr, v->free_counters, nb * 4, cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemcpy(st.queues, v->queues, nb * 4, cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemcpy(st.slots, v->slots, (uint64_t)st.total_slots * 4, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemset(st.spares, 0xFF, (uint64_t)st.total_slots * 4));  // the view holds none
   uint32_t *d_mc = nullptr;
   CUDA_TRY(cudaMalloc(&d_mc, nb * 4));
   cudaError_t e = cudaMemcpy(d_mc, v->malloc_counters, nb * 4, cudaMemcpyHostToDevice);
@@ -725,7 +749,7 @@ int gal_trim(gal_handle *h, void *stream) {
 int gal_malloc_batched(gal_handle *h, const uint64_t *sizes, uint64_t n, void **out, void *stream) {
   if (!h || (n && (!sizes || !out))) return GAL_ERR_ARGS;
   if (!n) return GAL_OK;
-  unsigned g = grid_for(n, BATCH_THREADS);
+  unsigned g = grid_for(n, BATCH_WORKERS);
   unsigned p = (unsigned)persistent_grid(h->device, k_malloc_batched);
   k_malloc_batched<<<g < p ? g : p, BATCH_THREADS, 0, (cudaStream_t)stream>>>(h->d_state, sizes, n, out);
   CUDA_TRY(cudaGetLastError());

@@ -76,6 +76,7 @@ struct state {
   uint32_t total_slots;
   uint32_t gather_unlocked_below;  // see gal_config
   uint32_t team_width;             // see gal_config (1..32, a power of two)
+  uint32_t use_spares;             // see gal_config.spare_blocks
   uint32_t slot_base[GAL_MAX_TREES];
   uint32_t slot_count[GAL_MAX_TREES];
   veb_shape veb;
@@ -90,6 +91,8 @@ struct state {
   uint32_t *fctr;                // [S << bps_shift] frees counted
   uint32_t *queues;              // [S << bps_shift] recycle ring (block ids)
   uint32_t *slots;               // [total_slots] pinned blocks
+  uint32_t *spares;              // [total_slots] next block per slot, prepared ahead
+                                 // for the CTA-aggregated claims (NOBLK: none)
   uint32_t *locks;               // tree locks (bit t) + bit num_trees for runs
   uint32_t *error;               // GAL_DEV_ERR_* bits
 };

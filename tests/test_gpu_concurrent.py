@@ -132,10 +132,11 @@ def test_churn_payloads(G, batched):
         g.close()
 
 
-def test_churn_e2e_payloads(G, torch):
+@pytest.mark.parametrize("spares", [0, 1])
+def test_churn_e2e_payloads(G, torch, spares):
     """The same churn through the public batched entry points, sizes copied
     from pinned host memory every round."""
-    g = G.Gallatin.generate_on_device(16 << 30, 42)
+    g = G.Gallatin.generate_on_device(16 << 30, 42, spare_blocks=spares)
     try:
         N, R = 1 << 18, 4
         sizes = torch.empty(N * R, dtype=torch.int64, pin_memory=True)
@@ -204,15 +205,36 @@ def test_everything_freed_then_trim_gives_fresh_trees(G, torch, batched):
         g.close()
 
 
-def test_churn_then_trim_gives_fresh_trees(G):
-    """The batched churn drains every allocation; after trim nothing of it remains."""
-    g = G.Gallatin.generate_on_device(16 << 30, 42)
+@pytest.mark.parametrize("spares", [0, 1])
+def test_churn_then_trim_gives_fresh_trees(G, spares):
+    """The batched churn drains every allocation; after trim nothing of it
+    remains, the spare blocks prepared by the service warps included."""
+    g = G.Gallatin.generate_on_device(16 << 30, 42, spare_blocks=spares)
     try:
         fresh = g.export()
         ms, r = g.bench_churn(1 << 18, 4, 1, True, True, 0, 1)
-        assert r.frees == r.mallocs_ok and r.error_word == 0
+        assert r.frees == r.mallocs_ok and r.error_word == 0 and r.payload_mismatch == 0
         g.trim()
+        assert g.error_word() == 0, g.error_info()
         assert g.export().diff(fresh, fields=TREE_FIELDS) == []
+    finally:
+        g.close()
+
+
+@pytest.mark.parametrize("mode", [1, 1 | (1 << 4), 1 | (2 << 4), 3])
+def test_churn_spare_blocks_and_requests_per_thread(G, mode):
+    """Spare blocks on, 1, 2 or 4 requests per thread per CTA iteration, and
+    the CTA-hash free: the same payload and accounting invariants, per-SM
+    slots and 64 MiB segments as in the headline step."""
+    g = G.Gallatin.generate_on_device(32 << 30, 42, spare_blocks=1, pinned_slots_first=0,
+                                      bytes_per_segment=64 << 20, gather_unlocked_below=16)
+    try:
+        N, R = 1 << 19, 6
+        ms, r = g.bench_churn(N, R, 1, mode, True, 1, 2)
+        assert r.mallocs_ok == 2 * N * R and r.mallocs_failed == 0
+        assert r.payload_mismatch == 0
+        assert r.frees == r.mallocs_ok
+        assert r.error_word == 0
     finally:
         g.close()
 
