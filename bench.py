@@ -72,7 +72,9 @@ def parse():
                    help="batched form: frees combined per CTA (shared-memory hash) or per warp team")
     p.add_argument("--quick", action="store_true", help="headline batched steps only (profiling)")
     p.add_argument("--configs", action="store_true",
-                   help="instead of the headline: BASELINE configs 1, 3 and 5, one JSON line")
+                   help="instead of the headline: the secondary workloads (tid stamp, serial "
+                        "trace, large and block-size allocations, served loop, hash tables), "
+                        "one JSON line")
     return p.parse_args()
 
 

@@ -233,8 +233,8 @@ __global__ void __launch_bounds__(BATCH_THREADS)
   gal::cta_workers_done(sm);
 }
 
-// Batched free: each thread takes FREE_PER_THREAD consecutive entries per
-// pass of a persistent grid and frees them with gal::free_n (table lookups and
+// Batched free: each thread takes FREE_PER_THREAD entries per pass of a
+// persistent grid and frees them with gal::free_n (table lookups and
 // free-counter atomics issued back to back, warp teams per block).  The list
 // holds n entries, or *d_count when that is given and smaller (a count that
 // an earlier kernel on the stream wrote).
@@ -244,14 +244,20 @@ __global__ void __launch_bounds__(BATCH_THREADS)
     k_free_batched(const gal::state *s, void *const *ptrs, uint64_t n,
                    const unsigned long long *d_count) {
   if (d_count && *d_count < n) n = *d_count;
-  const uint64_t stride = (uint64_t)gridDim.x * BATCH_THREADS * FREE_PER_THREAD;
-  for (uint64_t i0 = ((uint64_t)blockIdx.x * BATCH_THREADS + threadIdx.x) * FREE_PER_THREAD; i0 < n;
-       i0 += stride) {
+  // a warp takes 32 x FREE_PER_THREAD consecutive entries; lane l holds entries
+  // l, l + 32, ... so neighbouring lanes hold neighbouring entries (which share
+  // blocks) in each of the FREE_PER_THREAD team formations
+  const uint64_t per_warp = 32ull * FREE_PER_THREAD;
+  const uint64_t warp = ((uint64_t)blockIdx.x * BATCH_THREADS + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * BATCH_THREADS) >> 5;
+  const uint32_t lane = threadIdx.x & 31u;
+  for (uint64_t w0 = warp * per_warp; w0 < n; w0 += nwarps * per_warp) {
     void *p[FREE_PER_THREAD];
     bool go[FREE_PER_THREAD];
 #pragma unroll
     for (int k = 0; k < FREE_PER_THREAD; k++) {
-      p[k] = i0 + k < n ? ptrs[i0 + k] : nullptr;
+      const uint64_t i = w0 + (uint64_t)k * 32u + lane;
+      p[k] = i < n ? ptrs[i] : nullptr;
       go[k] = p[k] != nullptr;
     }
     gal::free_n<FREE_PER_THREAD>(s, p, go);
