@@ -309,3 +309,108 @@ extern "C" int dropin_poison_test(uint64_t num_bytes, uint64_t n, uint64_t bytes
   out[4] = err;
   return e == cudaSuccess ? 0 : 1;
 }
+
+// ---- divergent calls in data-dependent loops (the reference's threading
+// contract: any subset of a warp's lanes may call malloc/free, in loops)
+
+__device__ __forceinline__ uint64_t mixbits(uint64_t z) {
+  z ^= z >> 31;
+  z *= 0x7FB5D329728EA185ull;
+  z ^= z >> 27;
+  return z;
+}
+
+// thread t runs (h % 7) iterations; in each it allocates a size drawn from h,
+// stamps it, and frees the previous allocation on odd draws (so lanes of a
+// warp call malloc and free at different times, some exiting early).  The
+// live allocations at the end stay in bits[t * 8 + j] with their sizes.
+__global__ void divergent_loops(uint64_t n, uint64_t **bits, uint64_t *sizes, unsigned long long *c) {
+  uint64_t tid = threadIdx.x + (uint64_t)blockIdx.x * blockDim.x;
+  if (tid >= n) return;
+  uint64_t h = mixbits(tid * 0x9E3779B97F4A7C15ull + 1);
+  if ((h & 15) == 0) return;  // some lanes never call
+  const int iters = (int)(h % 7);
+  uint64_t *prev = nullptr;
+  int kept = 0;
+  for (int i = 0; i < iters; i++) {
+    h = mixbits(h + i);
+    uint64_t size = 16ull << (h % 9);  // 16 B .. 4 KiB
+    if (h & 32) size += (h >> 8) % 17;  // and some in between
+    uint64_t *p = (uint64_t *)global_malloc(size);
+    if (!p) continue;
+    atomicAdd(&c[0], 1ull);
+    p[0] = tid;
+    p[(size / 8) - 1 > 0 ? (size / 8) - 1 : 0] = ~tid;
+    if ((h & 1) && prev) {
+      if (prev[0] != tid) atomicAdd(&c[1], 1ull);
+      global_free(prev);
+      prev = nullptr;
+    }
+    if (prev && kept < 8) {  // keep it for the host's overlap check
+      bits[tid * 8 + kept] = prev;
+      sizes[tid * 8 + kept] = 0;  // filled below
+      kept++;
+    }
+    prev = p;
+    if (kept < 8) sizes[tid * 8 + kept] = size;
+  }
+  if (prev && kept < 8) bits[tid * 8 + kept] = prev;
+}
+
+__global__ void divergent_check_free(uint64_t n, uint64_t **bits, unsigned long long *c) {
+  uint64_t i = threadIdx.x + (uint64_t)blockIdx.x * blockDim.x;
+  if (i >= n * 8) return;
+  uint64_t *p = bits[i];
+  if (!p) return;
+  if (p[0] != i / 8) atomicAdd(&c[1], 1ull);
+  global_free(p);
+}
+
+// out[0] successful mallocs, [1] stamp mismatches, [2] overlapping live
+// allocations (checked on the host), [3] device error word
+extern "C" int dropin_divergent_test(uint64_t num_bytes, uint64_t n, int rounds, uint64_t *out) {
+  init_global_allocator(num_bytes, 42, false);
+  uint64_t **bits = nullptr;
+  uint64_t *sizes = nullptr;
+  unsigned long long *c = nullptr;
+  cudaMalloc(&bits, n * 8 * sizeof(uint64_t *));
+  cudaMalloc(&sizes, n * 8 * sizeof(uint64_t));
+  cudaMalloc(&c, 4 * sizeof(unsigned long long));
+  cudaMemset(c, 0, 4 * sizeof(unsigned long long));
+  uint64_t overlaps = 0;
+  cudaError_t e = cudaSuccess;
+  for (int r = 0; r < rounds && e == cudaSuccess; r++) {
+    cudaMemset(bits, 0, n * 8 * sizeof(uint64_t *));
+    cudaMemset(sizes, 0, n * 8 * sizeof(uint64_t));
+    divergent_loops<<<(unsigned)((n + 255) / 256), 256>>>(n, bits, sizes, c);
+    e = cudaDeviceSynchronize();
+    // live ranges [p, p + 16) at least: no two live pointers may coincide
+    uint64_t *hb = (uint64_t *)malloc(n * 8 * sizeof(uint64_t));
+    cudaMemcpy(hb, bits, n * 8 * sizeof(uint64_t), cudaMemcpyDeviceToHost);
+    uint64_t m = 0;
+    for (uint64_t i = 0; i < n * 8; i++)
+      if (hb[i]) hb[m++] = hb[i];
+    qsort(hb, m, sizeof(uint64_t), [](const void *a, const void *b) {
+      uint64_t x = *(const uint64_t *)a, y = *(const uint64_t *)b;
+      return x < y ? -1 : (x > y ? 1 : 0);
+    });
+    for (uint64_t i = 1; i < m; i++)
+      if (hb[i] < hb[i - 1] + 16) overlaps++;
+    free(hb);
+    divergent_check_free<<<(unsigned)((n * 8 + 255) / 256), 256>>>(n, bits, c);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  }
+  unsigned long long h[4] = {0, 0, 0, 0};
+  cudaMemcpy(h, c, sizeof(h), cudaMemcpyDeviceToHost);
+  uint32_t err = 0;
+  gal_last_error(gal_global(), &err);
+  cudaFree(bits);
+  cudaFree(sizes);
+  cudaFree(c);
+  free_global_allocator();
+  out[0] = h[0];
+  out[1] = h[1];
+  out[2] = overlaps;
+  out[3] = err;
+  return e == cudaSuccess ? 0 : 1;
+}
