@@ -21,7 +21,9 @@ failure.  The arena is 128 GiB (2x that) for both arms.
 persistent kernels, each step one captured CUDA graph); `e2e` is the same churn
 through the public C ABI entry points (gal_malloc_batched / gal_free_batched)
 with each round's request sizes copied from pinned host memory inside the
-timed region.  The plain per-thread path is reported beside it.
+timed region.  The plain per-thread path is reported beside it, at the
+reference's knobs (128 pinned slots halving to 4, 16 MiB segments) and at
+the batched form's knobs.
 Multi-GPU: replicas only (each rank its own allocator; no collective on the
 data path); `value` sums all ranks' ops over the slowest rank's time.
 """
@@ -463,6 +465,16 @@ def main():
     latency["plain"] = lat(gp, False)
     errors |= gp.error_word()
     gp.close()
+    # the same per-thread calls on the batched form's knobs
+    gt = G.Gallatin.generate_on_device(arena, ALLOC_SEED, **tuned)
+    _, plain_t = gt.bench_churn(N, R, SEED, batched=False, use_graph=True,
+                                warmup=1, steps=max(1, args.steps // 2))
+    plain_tuned_v = (plain_t.mallocs_ok + plain_t.frees) / (plain_t.ms_total / 1e3)
+    latency["plain_tuned_knobs"] = lat(gt, False)
+    errors |= gt.error_word() | plain_t.error_word
+    if plain_t.mallocs_failed or plain_t.payload_mismatch:
+        errors |= 1 << 31
+    gt.close()
 
     if rank != 0:
         return
@@ -480,6 +492,8 @@ def main():
                    "arena_bytes": arena, "threads_per_round": N, "rounds": R,
                    "l2": "no flush needed: 512 MiB pointer table and 16 GiB arena exceed the 129 MB L2",
                    "plain_ops_per_s": plain_v, "batched_over_plain": value / plain_v / world,
+                   "plain_tuned_knobs_ops_per_s": plain_tuned_v,
+                   "batched_over_plain_tuned_knobs": value / plain_tuned_v / world,
                    "mallocs_per_step": per_step_mallocs, "mallocs_failed": res.mallocs_failed,
                    "payload_mismatch": res.payload_mismatch, "device_error_word": errors,
                    "wall_s_timed": wall},

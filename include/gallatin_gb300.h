@@ -73,13 +73,16 @@ typedef struct gal_config {
                                    reference's coalesced teams)                  */
   uint32_t arena_kind;          /* GAL_ARENA_*: where the arena lives; metadata
                                    is always device memory                       */
-  uint32_t spare_blocks;        /* 1: the CTA-aggregated (batched) claims keep
-                                   the next block of every pinned slot prepared
-                                   by a service warp, so a block running out is
-                                   replaced by one swap instead of a search of
-                                   the class's segments on the claim's path
-                                   (costs one block per slot held in reserve;
-                                   per-thread calls never use it)               */
+  uint32_t spare_blocks;        /* 1: every pinned slot keeps its next block
+                                   prepared, so a block running out is replaced
+                                   by one swap instead of a search of the
+                                   class's segments on the claim's path (the
+                                   CTA-aggregated kernels refill spares from a
+                                   service warp, per-thread calls from the lane
+                                   that swapped, after its team has gone on).
+                                   Costs one block per slot held in reserve;
+                                   serial offsets then differ from the
+                                   reference's.  0 = the reference's behaviour. */
 } gal_config;
 
 /* Arena backing (gal_config.arena_kind). */

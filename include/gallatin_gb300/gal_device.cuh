@@ -92,7 +92,7 @@ struct state {
   uint32_t *queues;              // [S << bps_shift] recycle ring (block ids)
   uint32_t *slots;               // [total_slots] pinned blocks
   uint32_t *spares;              // [total_slots] next block per slot, prepared ahead
-                                 // for the CTA-aggregated claims (NOBLK: none)
+                                 // (gal_config.spare_blocks; NOBLK: none)
   uint32_t *locks;               // tree locks (bit t) + bit num_trees for runs
   uint32_t *error;               // GAL_DEV_ERR_* bits
 };
@@ -679,6 +679,31 @@ GAL_DEVICE_COLD bool replace_block(const state *s, uint32_t tree, uint32_t slot,
   return true;
 }
 
+// Spare blocks (gal_config.spare_blocks): the slot's prepared next block is
+// swapped in with one CAS, so other warps see a fresh block at once instead of
+// an empty slot for the length of a segment search; the search then refills
+// the spare.  swap_spare returns whether the caller should refill (it falls
+// back to replace_block when no spare was ready).
+GAL_DEVICE_COLD bool swap_spare(const state *s, uint32_t tree, uint32_t slot, uint32_t blk, uint64_t tid) {
+  const uint32_t si = s->slot_base[tree] + slot;
+  const uint32_t nx = atomicExch(s->spares + si, NOBLK);
+  if (nx == NOBLK) {
+    replace_block(s, tree, slot, blk, tid);
+  } else if (atomicCAS(s->slots + si, blk, nx) != blk) {
+    credit_frees(s, nx, SLICES_PER_BLOCK);  // the slot moved on: give the spare back
+    return false;
+  }
+  return true;
+}
+GAL_DEVICE_COLD void refill_spare(const state *s, uint32_t tree, uint32_t slot, uint64_t tid) {
+  const uint32_t si = s->slot_base[tree] + slot;
+  if (ld_rlx(s->spares + si) != NOBLK) return;
+  const uint32_t nb = request_block(s, tree, tid);
+  if (nb == NOBLK) return;
+  __threadfence();
+  if (atomicCAS(s->spares + si, NOBLK, nb) != NOBLK) credit_frees(s, nb, SLICES_PER_BLOCK);
+}
+
 // Gallatin::boot_block (gallatin.cuh:726-787)
 GAL_DEVICE_COLD bool boot_block(const state *s, uint32_t tree, uint32_t slot, uint64_t tid) {
   if (slot >= s->slot_count[tree]) return false;
@@ -739,8 +764,13 @@ GAL_DEVICE_INLINE void *malloc_slices(const state *s, uint32_t tree, uint32_t co
     uint32_t leftover = start_valid ? (end_valid ? count - 1 : (uint32_t)(SLICES_PER_BLOCK - alloc)) : 0;
     if (leftover) credit_frees(s, blk, leftover);  // block_correct_frees
     const uint32_t rep = __ballot_sync(live, should_replace) & team;
-    if (rep && (int)lane == leader) replace_block(s, tree, slot, blk, tid);
+    bool refill = false;
+    if (rep && (int)lane == leader) {
+      if (s->use_spares) refill = swap_spare(s, tree, slot, blk, tid);
+      else replace_block(s, tree, slot, blk, tid);
+    }
     __syncwarp(live);
+    if (refill) refill_spare(s, tree, slot, tid);  // the team's other lanes go on
     if (start_valid && end_valid) {
       if ((uint32_t)(old >> 32) == tree) return slice_ptr(s, blk, alloc, tree);
       credit_frees(s, blk, 1);  // Block::check_valid failed: give the slice back
