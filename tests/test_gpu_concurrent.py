@@ -295,3 +295,41 @@ def test_double_free_is_reported_not_trapped(G, torch):
         assert g.error_word() == 0, g.error_info()
     finally:
         g.close()
+
+
+def test_wait_on_a_lock_nobody_releases_times_out(G, torch):
+    """Failure detection without a GPU fault: a class lock that nothing will
+    release (set through the state import) makes the segment gather's bounded
+    wait give up.  The request returns null, the error word carries TIMEOUT,
+    the context stays usable, and the same request succeeds once the lock is
+    released."""
+    from gallatin_gb300._abi import GAL_DEV_ERR_TIMEOUT
+    g = G.Gallatin.generate_on_device(1 << 30, 42, spin_limit=64)
+    try:
+        sv = g.export()
+        sv.locks = 0x3FF                   # every class lock and the run lock held
+        g.load(sv)
+        # two whole 16 MiB blocks of the largest class: the segment gathered
+        # ahead at boot serves one, the other needs a gather behind the lock
+        sizes = torch.full((2,), 16 << 20, dtype=torch.int64, device="cuda")
+        ptrs = torch.zeros(2, dtype=torch.int64, device="cuda")
+        g.malloc_per_thread(sizes, ptrs)
+        torch.cuda.synchronize()
+        p = ptrs.cpu().numpy()
+        assert (p != 0).sum() == 1
+        assert g.error_word() & GAL_DEV_ERR_TIMEOUT
+        g.free_per_thread(ptrs)
+        sv = g.export()
+        sv.locks = 0
+        g.load(sv)
+        g.clear_error()
+        one = torch.full((1,), 16 << 20, dtype=torch.int64, device="cuda")
+        got = torch.zeros(1, dtype=torch.int64, device="cuda")
+        g.malloc_per_thread(one, got)
+        torch.cuda.synchronize()
+        assert int(got.cpu()[0]) != 0
+        assert g.error_word() == 0, g.error_info()
+        g.free_per_thread(got)
+        torch.cuda.synchronize()
+    finally:
+        g.close()
