@@ -440,20 +440,44 @@ def main():
     # atomic peak.
     distinct, same = G.atomic_peak()
     per_step_mallocs = res.mallocs_ok / args.steps
-    if res.ms_malloc_kernels >= res.ms_free_kernels:
-        kern, ms_k, n_launch, units = ("k_churn_malloc_batched", res.ms_malloc_kernels,
-                                       res.malloc_launches, res.mallocs_ok)
-        alg_bytes = 12.0 * res.mallocs_ok
-    else:
-        kern, ms_k, n_launch, units = (
-            "k_churn_free_batched" if args.free_mode == "cta" else "k_churn_free_plain",
-            res.ms_free_kernels, res.free_launches, res.frees)
-        alg_bytes = 8.0 * N * R * (R + 1) / 2 * args.steps + 12.0 * res.frees
-    avg_launch_s = ms_k / 1e3 / n_launch
-    achieved = (units / n_launch) / avg_launch_s
-    hbm_achieved = (alg_bytes / n_launch) / avg_launch_s
     hbm_peak, peak_src = measured_hbm_peak()
-    traffic = read_profile_traffic(kern)
+    free_kern = "k_churn_free_batched" if args.free_mode == "cta" else "k_churn_free_plain"
+    phases = {
+        "k_churn_malloc_batched": (res.ms_malloc_kernels, res.malloc_launches, res.mallocs_ok,
+                                   12.0 * res.mallocs_ok),
+        free_kern: (res.ms_free_kernels, res.free_launches, res.frees,
+                    8.0 * N * R * (R + 1) / 2 * args.steps + 12.0 * res.frees),
+    }
+
+    def roofline_of(kern):
+        ms_k, n_launch, units, alg_bytes = phases[kern]
+        avg_launch_s = ms_k / 1e3 / n_launch
+        achieved = (units / n_launch) / avg_launch_s
+        hbm_achieved = (alg_bytes / n_launch) / avg_launch_s
+        traffic = read_profile_traffic(kern)
+        return {"bound": "hbm", "kernel": kern, "achieved": hbm_achieved / 1e9,
+                "peak": hbm_peak, "unit": "GB/s", "frac": hbm_achieved / 1e9 / hbm_peak,
+                "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes / n_launch,
+                "launch_ms": avg_launch_s * 1e3,
+                # the DRAM bytes ncu counted per launch over this run's launch time:
+                # what the memory system moved (scattered 4 B payload accesses
+                # move whole sectors)
+                "dram_traffic_gbs": traffic / avg_launch_s / 1e9 if traffic else None,
+                "dram_traffic_frac": traffic / avg_launch_s / 1e9 / hbm_peak if traffic else None,
+                "peak_source": peak_src,
+                "l2_atomic": {"achieved": achieved / 1e9, "peak": distinct / 1e9,
+                              "unit": "Gatomic/s", "frac": achieved / distinct,
+                              "atomics_per_unit": 1,
+                              "peak_source": "measured in this run: atomicAdd.u32 with return, "
+                                             "distinct addresses in a 32 MiB L2-resident buffer",
+                              "same_address_peak": same / 1e9}}
+
+    dominant = ("k_churn_malloc_batched" if res.ms_malloc_kernels >= res.ms_free_kernels
+                else free_kern)
+    roofline = roofline_of(dominant)
+    roofline["other_phase"] = {k: v for k, v in roofline_of(
+        free_kern if dominant == "k_churn_malloc_batched" else "k_churn_malloc_batched").items()
+        if k not in ("peak_source",)}
     errors = g.error_word()
     g.close()
 
@@ -484,7 +508,7 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic (Philox4x32-10 seed 1; sizes log-uniform 16 B-4 KiB rounded to pow2)",
         "config": {"workload": WORKLOAD, "path": "batched: CTA-aggregated persistent kernels, one CUDA graph per step",
-                   "pinned_slots_batched": args.slots or "one per SM", "pinned_slots_plain": "128 halving to 4",
+                   "pinned_slots_batched": args.slots or "one per SM", "pinned_slots_plain": "128 halving to 4 (default config: 16 MiB segments, lock-free gathers below 16 blocks per segment, no spare blocks)",
                    "batched_knobs": {"gather_unlocked_below": args.unlocked, "segment_mib": args.segment_mib,
                                      "spare_blocks": args.spares,
                                      "min_size": args.min_size, "max_size": args.max_size,
@@ -497,16 +521,7 @@ def main():
                    "mallocs_per_step": per_step_mallocs, "mallocs_failed": res.mallocs_failed,
                    "payload_mismatch": res.payload_mismatch, "device_error_word": errors,
                    "wall_s_timed": wall},
-        "roofline": {"bound": "hbm", "kernel": kern, "achieved": hbm_achieved / 1e9,
-                     "peak": hbm_peak, "unit": "GB/s", "frac": hbm_achieved / 1e9 / hbm_peak,
-                     "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes / n_launch,
-                     "peak_source": peak_src,
-                     "l2_atomic": {"achieved": achieved / 1e9, "peak": distinct / 1e9,
-                                   "unit": "Gatomic/s", "frac": achieved / distinct,
-                                   "atomics_per_unit": 1,
-                                   "peak_source": "measured in this run: atomicAdd.u32 with return, "
-                                                  "distinct addresses in a 32 MiB L2-resident buffer",
-                                   "same_address_peak": same / 1e9}},
+        "roofline": roofline,
         "e2e": {"value": e2e_v, "unit": "ops/s", "h2d_bytes_per_step": int(eres.h2d_bytes),
                 "d2h_bytes_per_step": int(eres.d2h_bytes),
                 "path": "gal_malloc_batched/gal_free_batched C ABI, sizes H2D from pinned host each round"},

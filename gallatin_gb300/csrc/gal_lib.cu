@@ -495,7 +495,7 @@ int gal_config_default(gal_config *cfg) {
   cfg->pinned_slots_min = 4;
   cfg->zero_arena = 1;
   cfg->spin_limit = 1u << 16;  // x backoff capped at 4 us: ~0.27 s per wait at most
-  cfg->gather_unlocked_below = 0;
+  cfg->gather_unlocked_below = 16;  // serially the lock is always free: same offsets
   cfg->team_width = 32;
   cfg->arena_kind = GAL_ARENA_DEVICE;
   cfg->spare_blocks = 0;

@@ -65,7 +65,12 @@ typedef struct gal_config {
   uint32_t spin_limit;          /* iteration cap for every device spin-wait       */
   uint32_t gather_unlocked_below; /* size classes with fewer blocks per segment
                                    gather segments without the class lock
-                                   (0 = always lock, as gallatin.cuh:1538)       */
+                                   (default 16; 0 = always lock, as
+                                   gallatin.cuh:1538).  One thread alone always
+                                   finds the lock free, so serial offsets are
+                                   the reference's either way; concurrently,
+                                   classes whose blocks fill a segment in a few
+                                   replacements stop queueing on the lock.     */
   uint32_t team_width;          /* aggregation width of per-thread claims and
                                    frees: lanes that share one atomic come from
                                    aligned groups of this many (1..32, a power

@@ -304,7 +304,7 @@ def test_wait_on_a_lock_nobody_releases_times_out(G, torch):
     the context stays usable, and the same request succeeds once the lock is
     released."""
     from gallatin_gb300._abi import GAL_DEV_ERR_TIMEOUT
-    g = G.Gallatin.generate_on_device(1 << 30, 42, spin_limit=64)
+    g = G.Gallatin.generate_on_device(1 << 30, 42, spin_limit=64, gather_unlocked_below=0)
     try:
         sv = g.export()
         sv.locks = 0x3FF                   # every class lock and the run lock held
