@@ -312,15 +312,24 @@ GAL_DEVICE_COLD uint64_t veb_malloc_first(const veb_ref &v) {
 }
 
 // veb_tree::find_random_valid_index (veb.cuh:946-977)
+// A search that came back empty from `start` shows that no item lies in
+// [start, U); later attempts starting at or above the lowest such start are
+// answered from that without touching the tree (the result is the one the
+// reference's repeated searches give when nothing is inserted meanwhile, and
+// one of the outcomes its relaxed reads allow when something is).  A sparse
+// tree whose items sit at low ids otherwise costs all 15 attempts.
 GAL_DEVICE_COLD uint64_t veb_find_random(const veb_ref &v, uint64_t tid) {
   const uint64_t U = v.sh->items[v.sh->layers - 1];
   uint64_t h1 = murmur64a_u64(tid, v.seed);
   uint64_t h2 = murmur64a_u64(tid, h1);
+  uint64_t empty_from = U;  // no item in [empty_from, U)
   for (uint64_t a = 0; a < (uint64_t)VEB_ATTEMPTS; a++) {
     uint64_t start = (h1 + a * h2) % U;
+    if (start >= empty_from) continue;
     if (veb_query(v, start)) return start;
     uint64_t idx = veb_successor(v, start);
     if (idx != FAIL) return idx;
+    empty_from = start;
   }
   return veb_successor(v, 0);
 }
