@@ -443,7 +443,7 @@ int gal_bench_tables(gal_handle *h, uint32_t n_tables, const uint64_t *offsets, 
   uint64_t *d_off = nullptr;
   table_desc *d_desc = nullptr;
   unsigned long long *stats = nullptr, *d_keys = nullptr, *d_vals = nullptr, *d_n = nullptr;
-  cudaEvent_t ev[7] = {};
+  cudaEvent_t ev[8] = {};  // phase boundaries 0-5, teardown 6-7
   unsigned long long hs[S_N];
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
@@ -491,19 +491,12 @@ int gal_bench_tables(gal_handle *h, uint32_t n_tables, const uint64_t *offsets, 
     TK(cudaMemcpy(dump_keys, d_keys, got * 8, cudaMemcpyDeviceToHost));
     TK(cudaMemcpy(dump_vals, d_vals, got * 8, cudaMemcpyDeviceToHost));
   }
-  {
-    cudaEvent_t t0, t1;
-    TK(cudaEventCreate(&t0));
-    TK(cudaEventCreate(&t1));
-    TK(cudaEventRecord(t0));
-    k_tables_destroy<<<n_tables, TBT>>>(d, d_desc, stats);
-    TK(cudaGetLastError());
-    TK(cudaEventRecord(t1));
-    TK(cudaEventSynchronize(t1));
-    TK(cudaEventElapsedTime(&res->ms[5], t0, t1));
-    cudaEventDestroy(t0);
-    cudaEventDestroy(t1);
-  }
+  TK(cudaEventRecord(ev[6]));
+  k_tables_destroy<<<n_tables, TBT>>>(d, d_desc, stats);
+  TK(cudaGetLastError());
+  TK(cudaEventRecord(ev[7]));
+  TK(cudaEventSynchronize(ev[7]));
+  TK(cudaEventElapsedTime(&res->ms[5], ev[6], ev[7]));
   for (int k = 0; k < 5; k++) TK(cudaEventElapsedTime(&res->ms[k], ev[k], ev[k + 1]));
   TK(cudaMemcpy(hs, stats, sizeof(hs), cudaMemcpyDeviceToHost));
   res->total_pairs = total;
