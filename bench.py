@@ -415,7 +415,8 @@ def main():
     e2e_steps = max(2, args.steps // 2)
     barrier(world)
     torch.cuda.synchronize()
-    ems, eres = g.bench_churn_e2e(sizes.data_ptr(), N, R, SEED, warmup=1, steps=e2e_steps)
+    ems, eres = g.bench_churn_e2e(sizes.data_ptr(), N, R, SEED, warmup=1, steps=e2e_steps,
+                                  use_graph=True)
     torch.cuda.synchronize()
     barrier(world)
     esecs = max_over_ranks(eres.ms_total / 1e3, world)
@@ -524,7 +525,9 @@ def main():
         "roofline": roofline,
         "e2e": {"value": e2e_v, "unit": "ops/s", "h2d_bytes_per_step": int(eres.h2d_bytes),
                 "d2h_bytes_per_step": int(eres.d2h_bytes),
-                "path": "gal_malloc_batched/gal_free_batched C ABI, sizes H2D from pinned host each round"},
+                "path": "gal_malloc_batched / gal_free_batched_n C ABI with user stamp and selection "
+                        "kernels; each round's sizes copied H2D from pinned host memory, counters "
+                        "read back; the step captured once as a CUDA graph (two streams)"},
         "latency": latency,
         "gpu_launches": int(res.malloc_launches + res.free_launches),
         "clocks": clk.summary(),

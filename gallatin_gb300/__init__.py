@@ -117,7 +117,7 @@ def lib():
         "gal_free_batched_n": ([vp, vp, vp, u64, vp], C.c_int),
         "gal_trim": ([vp, vp], C.c_int),
         "gal_bench_churn": ([vp, u64, u32, u32, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp], C.c_int),
-        "gal_bench_churn_e2e": ([vp, vp, u64, u32, u32, C.c_int, C.c_int, vp, vp], C.c_int),
+        "gal_bench_churn_e2e": ([vp, vp, u64, u32, u32, C.c_int, C.c_int, vp, vp, C.c_int], C.c_int),
         "gal_churn_sizes": ([u64, u64, u32, vp], C.c_int),
         "gal_bench_stamp": ([vp, u64, u64, C.c_int, vp, vp], C.c_int),
         "gal_bench_latency": ([vp, u64, u32, C.c_int, vp, vp], C.c_int),
@@ -308,11 +308,11 @@ class Gallatin:
                "gal_bench_churn")
         return ms[:steps], r
 
-    def bench_churn_e2e(self, host_sizes, threads_per_round, rounds, seed, warmup, steps):
+    def bench_churn_e2e(self, host_sizes, threads_per_round, rounds, seed, warmup, steps, use_graph=False):
         ms = np.zeros(max(steps, 1), dtype=np.float32)
         r = ChurnResult()
         _check(lib().gal_bench_churn_e2e(self._h, _ptr(host_sizes), threads_per_round, rounds, seed,
-                                         warmup, steps, ms.ctypes.data, C.byref(r)),
+                                         warmup, steps, ms.ctypes.data, C.byref(r), int(use_graph)),
                "gal_bench_churn_e2e")
         return ms[:steps], r
 

@@ -478,10 +478,12 @@ done:
  * stream, two rounds ahead into two alternating buffers, and served by
  * gal_malloc_batched; a user kernel stamps the payloads; frees are selected by
  * a user kernel that compacts them into a list whose length stays on the
- * device, served by gal_free_batched_n; the step's counters are read back. */
+ * device, served by gal_free_batched_n; the step's counters are read back.
+ * use_graph: the step (both streams, copies included) is captured once as a
+ * CUDA graph, as a user replaying the same step would. */
 int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t threads_per_round,
                         uint32_t rounds, uint32_t seed, int warmup, int steps, float *step_ms,
-                        gal_churn_result *res) {
+                        gal_churn_result *res, int use_graph) {
   if (!h || !res || !host_sizes || !threads_per_round || !rounds) return GAL_ERR_ARGS;
   if (threads_per_round % galwl::SLOT_ALIGN) return GAL_ERR_ARGS;
   int rc = GAL_OK;
@@ -489,20 +491,67 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
   void **ptrs = nullptr, **freelist = nullptr;
   uint32_t *live = nullptr;
   uint64_t *d_sizes[2] = {nullptr, nullptr};
-  unsigned long long *stats = nullptr, *count = nullptr;
-  unsigned long long hst[4];
+  unsigned long long *stats = nullptr, *count = nullptr, *hst = nullptr;  // hst: pinned host
   cudaStream_t st = nullptr, cp = nullptr;
-  cudaEvent_t e0 = nullptr, e1 = nullptr, copied[2] = {nullptr, nullptr}, consumed[2] = {nullptr, nullptr};
+  cudaEvent_t e0 = nullptr, e1 = nullptr, fork = nullptr, copied[2] = {nullptr, nullptr},
+              consumed[2] = {nullptr, nullptr};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
   int dev = 0, sms = 0, per_sm = 0;
   memset(res, 0, sizeof(*res));
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_select_free_list, FREE_BT, 0);
   const uint64_t grid_sel = (uint64_t)sms * (per_sm > 0 ? per_sm : 1);
+  // one step on st (copies forked onto cp and joined back through the events)
+  auto enqueue = [&]() -> int {
+    if (cudaEventRecord(fork, st) != cudaSuccess || cudaStreamWaitEvent(cp, fork, 0) != cudaSuccess)
+      return GAL_ERR_CUDA;
+    for (uint32_t r = 0; r < rounds && r < 2; r++) {
+      if (cudaMemcpyAsync(d_sizes[r], host_sizes + (uint64_t)r * N, N * sizeof(uint64_t),
+                          cudaMemcpyHostToDevice, cp) != cudaSuccess ||
+          cudaEventRecord(copied[r], cp) != cudaSuccess)
+        return GAL_ERR_CUDA;
+    }
+    if (cudaMemsetAsync(stats, 0, 4 * sizeof(unsigned long long), st) != cudaSuccess) return GAL_ERR_CUDA;
+    for (uint32_t r = 0; r <= rounds; r++) {
+      const bool drain = r == rounds;
+      if (r > 0) {
+        const uint64_t nscan = drain ? nslots : N * r;
+        const uint64_t chunk = (uint64_t)(FREE_BT / 32) * galwl::WARP_SLOTS;
+        const unsigned g = (unsigned)std::min<uint64_t>((nscan + chunk - 1) / chunk, grid_sel);
+        if (cudaMemsetAsync(count, 0, sizeof(unsigned long long), st) != cudaSuccess) return GAL_ERR_CUDA;
+        k_select_free_list<<<g, FREE_BT, 0, st>>>(ptrs, live, freelist, count, nscan, r, seed,
+                                                  drain ? 1 : 0, stats);
+        int e = gal_free_batched_n(h, freelist, count, nscan, st);
+        if (e) return e;
+      }
+      if (drain) break;
+      const int b = (int)(r & 1u);
+      if (cudaStreamWaitEvent(st, copied[b], 0) != cudaSuccess) return GAL_ERR_CUDA;
+      int e = gal_malloc_batched(h, d_sizes[b], N, ptrs + (uint64_t)r * N, st);
+      if (e) return e;
+      if (cudaEventRecord(consumed[b], st) != cudaSuccess) return GAL_ERR_CUDA;
+      if (r + 2 < rounds) {  // refill this buffer with round r + 2 while the GPU works
+        if (cudaStreamWaitEvent(cp, consumed[b], 0) != cudaSuccess ||
+            cudaMemcpyAsync(d_sizes[b], host_sizes + (uint64_t)(r + 2) * N, N * sizeof(uint64_t),
+                            cudaMemcpyHostToDevice, cp) != cudaSuccess ||
+            cudaEventRecord(copied[b], cp) != cudaSuccess)
+          return GAL_ERR_CUDA;
+      }
+      k_stamp_payload<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(ptrs, live, (uint64_t)r * N, N,
+                                                                   seed, stats);
+    }
+    if (cudaMemcpyAsync(hst, stats, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st) !=
+        cudaSuccess)
+      return GAL_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? GAL_OK : GAL_ERR_CUDA;
+  };
   CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&cp, cudaStreamNonBlocking));
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
+  CK(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
   for (int b = 0; b < 2; b++) {
     CK(cudaEventCreateWithFlags(&copied[b], cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&consumed[b], cudaEventDisableTiming));
@@ -513,46 +562,27 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
   CK(cudaMalloc(&live, nslots / 8));
   CK(cudaMalloc(&stats, 4 * sizeof(unsigned long long)));
   CK(cudaMalloc(&count, sizeof(unsigned long long)));
+  CK(cudaMallocHost(&hst, 4 * sizeof(unsigned long long)));
   CK(cudaMemsetAsync(ptrs, 0, nslots * sizeof(void *), st));
   CK(cudaMemsetAsync(live, 0, nslots / 8, st));
+  CK(cudaStreamSynchronize(st));
+  if (use_graph) {
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+    int e = enqueue();
+    cudaError_t ce = cudaStreamEndCapture(st, &graph);
+    if (e) { rc = e; goto done; }
+    CK(ce);
+    CK(cudaGraphInstantiate(&exec, graph, 0));
+  }
   for (int s = 0; s < warmup + steps; s++) {
     CK(cudaStreamSynchronize(st));
     CK(cudaEventRecord(e0, st));
-    CK(cudaStreamWaitEvent(cp, e0, 0));
-    for (uint32_t r = 0; r < rounds && r < 2; r++) {
-      CK(cudaMemcpyAsync(d_sizes[r], host_sizes + (uint64_t)r * N, N * sizeof(uint64_t),
-                         cudaMemcpyHostToDevice, cp));
-      CK(cudaEventRecord(copied[r], cp));
-    }
-    CK(cudaMemsetAsync(stats, 0, sizeof(hst), st));
-    for (uint32_t r = 0; r <= rounds; r++) {
-      bool drain = r == rounds;
-      if (r > 0) {
-        uint64_t nscan = drain ? nslots : N * r;
-        const uint64_t chunk = (uint64_t)(FREE_BT / 32) * galwl::WARP_SLOTS;
-        unsigned g = (unsigned)std::min<uint64_t>((nscan + chunk - 1) / chunk, grid_sel);
-        CK(cudaMemsetAsync(count, 0, sizeof(unsigned long long), st));
-        k_select_free_list<<<g, FREE_BT, 0, st>>>(ptrs, live, freelist, count, nscan, r, seed,
-                                                  drain ? 1 : 0, stats);
-        int e = gal_free_batched_n(h, freelist, count, nscan, st);
-        if (e) { rc = e; goto done; }
-      }
-      if (drain) break;
-      const int b = (int)(r & 1u);
-      CK(cudaStreamWaitEvent(st, copied[b], 0));
-      int e = gal_malloc_batched(h, d_sizes[b], N, ptrs + (uint64_t)r * N, st);
+    if (use_graph) {
+      CK(cudaGraphLaunch(exec, st));
+    } else {
+      int e = enqueue();
       if (e) { rc = e; goto done; }
-      CK(cudaEventRecord(consumed[b], st));
-      if (r + 2 < rounds) {  // refill this buffer with round r + 2 while the GPU works
-        CK(cudaStreamWaitEvent(cp, consumed[b], 0));
-        CK(cudaMemcpyAsync(d_sizes[b], host_sizes + (uint64_t)(r + 2) * N, N * sizeof(uint64_t),
-                           cudaMemcpyHostToDevice, cp));
-        CK(cudaEventRecord(copied[b], cp));
-      }
-      k_stamp_payload<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(ptrs, live, (uint64_t)r * N, N, seed,
-                                                                   stats);
     }
-    CK(cudaMemcpyAsync(hst, stats, sizeof(hst), cudaMemcpyDeviceToHost, st));
     CK(cudaEventRecord(e1, st));
     CK(cudaEventSynchronize(e1));
     CK(cudaGetLastError());
@@ -571,13 +601,16 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
     }
   }
   res->h2d_bytes = nslots * sizeof(uint64_t);
-  res->d2h_bytes = sizeof(hst);
+  res->d2h_bytes = 4 * sizeof(unsigned long long);
   gal_last_error(h, &res->error_word);
 done:
   if (st) cudaStreamSynchronize(st);
   if (cp) cudaStreamSynchronize(cp);
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
+  if (fork) cudaEventDestroy(fork);
   for (int b = 0; b < 2; b++) {
     if (copied[b]) cudaEventDestroy(copied[b]);
     if (consumed[b]) cudaEventDestroy(consumed[b]);
@@ -588,6 +621,7 @@ done:
   if (freelist) cudaFree(freelist);
   if (stats) cudaFree(stats);
   if (count) cudaFree(count);
+  if (hst) cudaFreeHost(hst);
   if (st) cudaStreamDestroy(st);
   if (cp) cudaStreamDestroy(cp);
   return rc;

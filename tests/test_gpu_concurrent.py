@@ -132,16 +132,16 @@ def test_churn_payloads(G, batched):
         g.close()
 
 
-@pytest.mark.parametrize("spares", [0, 1])
-def test_churn_e2e_payloads(G, torch, spares):
+@pytest.mark.parametrize("spares,graph", [(0, False), (1, False), (1, True)])
+def test_churn_e2e_payloads(G, torch, spares, graph):
     """The same churn through the public batched entry points, sizes copied
-    from pinned host memory every round."""
+    from pinned host memory every round (and the step captured as a graph)."""
     g = G.Gallatin.generate_on_device(16 << 30, 42, spare_blocks=spares)
     try:
         N, R = 1 << 18, 4
         sizes = torch.empty(N * R, dtype=torch.int64, pin_memory=True)
         sizes.numpy()[:] = G.churn_sizes(0, N * R, 1).view(np.int64)
-        ms, r = g.bench_churn_e2e(sizes.data_ptr(), N, R, 1, 1, 2)
+        ms, r = g.bench_churn_e2e(sizes.data_ptr(), N, R, 1, 1, 2, use_graph=graph)
         assert r.mallocs_ok == 2 * N * R and r.mallocs_failed == 0
         assert r.payload_mismatch == 0
         assert r.frees == r.mallocs_ok
