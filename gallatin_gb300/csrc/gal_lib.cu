@@ -25,6 +25,7 @@ struct gal_handle {
   char *arena = nullptr;
   uint64_t arena_bytes = 0;
   gal_state_dims dims{};
+  int grid_malloc = 0, grid_free = 0;  // persistent grids of the batched kernels (0: not yet known)
 };
 
 namespace {
@@ -756,7 +757,8 @@ int gal_malloc_batched(gal_handle *h, const uint64_t *sizes, uint64_t n, void **
   if (!h || (n && (!sizes || !out))) return GAL_ERR_ARGS;
   if (!n) return GAL_OK;
   unsigned g = grid_for(n, BATCH_WORKERS);
-  unsigned p = (unsigned)persistent_grid(h->device, k_malloc_batched);
+  if (!h->grid_malloc) h->grid_malloc = persistent_grid(h->device, k_malloc_batched);
+  unsigned p = (unsigned)h->grid_malloc;
   k_malloc_batched<<<g < p ? g : p, BATCH_THREADS, 0, (cudaStream_t)stream>>>(h->d_state, sizes, n, out);
   CUDA_TRY(cudaGetLastError());
   return GAL_OK;
@@ -771,7 +773,8 @@ int gal_free_batched_n(gal_handle *h, void *const *ptrs, const unsigned long lon
   if (!h || (max_n && !ptrs)) return GAL_ERR_ARGS;
   if (!max_n) return GAL_OK;
   unsigned g = grid_for((max_n + FREE_PER_THREAD - 1) / FREE_PER_THREAD, BATCH_THREADS);
-  unsigned p = (unsigned)persistent_grid(h->device, k_free_batched);
+  if (!h->grid_free) h->grid_free = persistent_grid(h->device, k_free_batched);
+  unsigned p = (unsigned)h->grid_free;
   k_free_batched<<<g < p ? g : p, BATCH_THREADS, 0, (cudaStream_t)stream>>>(h->d_state, ptrs, max_n,
                                                                             d_count);
   CUDA_TRY(cudaGetLastError());
