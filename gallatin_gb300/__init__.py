@@ -110,6 +110,7 @@ def lib():
         "gal_teardown": ([], C.c_int),
         "gal_global": ([], vp),
         "gal_replay_trace": ([vp, vp, u64, vp, vp, vp], C.c_int),
+        "gal_replay_warp_trace": ([vp, vp, u64, vp, vp, vp], C.c_int),
         "gal_malloc_per_thread": ([vp, vp, u64, vp, vp], C.c_int),
         "gal_free_per_thread": ([vp, vp, u64, vp], C.c_int),
         "gal_malloc_batched": ([vp, vp, u64, vp, vp], C.c_int),
@@ -271,6 +272,20 @@ class Gallatin:
         d_smid = torch.zeros(1, dtype=torch.int32, device="cuda")
         _check(lib().gal_replay_trace(self._h, d_ops.data_ptr(), len(ops), d_out.data_ptr(),
                                       d_smid.data_ptr(), None), "gal_replay_trace")
+        torch.cuda.synchronize()
+        return d_out.cpu().numpy().view(np.uint64), int(d_smid.item())
+
+    def replay_warp(self, steps: np.ndarray):
+        """Warp-wide calls replayed by one warp (33 words per step); returns
+        (32 offsets per step, smid)."""
+        import torch
+        steps = np.ascontiguousarray(steps, dtype=np.uint64)
+        n = len(steps) // 33
+        d_steps = torch.from_numpy(steps.view(np.int64)).cuda()
+        d_out = torch.full((n * 32,), -1, dtype=torch.int64, device="cuda")
+        d_smid = torch.zeros(1, dtype=torch.int32, device="cuda")
+        _check(lib().gal_replay_warp_trace(self._h, d_steps.data_ptr(), n, d_out.data_ptr(),
+                                           d_smid.data_ptr(), None), "gal_replay_warp_trace")
         torch.cuda.synchronize()
         return d_out.cpu().numpy().view(np.uint64), int(d_smid.item())
 

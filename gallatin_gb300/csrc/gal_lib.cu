@@ -195,6 +195,37 @@ __global__ void k_replay(const gal::state *s, const uint64_t *ops, uint64_t nops
   }
 }
 
+// warp-wide calls by one warp (gal_replay_warp_trace)
+__global__ void k_replay_warp(const gal::state *s, const uint64_t *steps, uint64_t nsteps,
+                              uint64_t *out, uint32_t *out_smid) {
+  if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+  const uint32_t lane = threadIdx.x;
+  if (lane == 0) out_smid[0] = gal::sm_id();
+  for (uint64_t i = 0; i < nsteps; i++) {
+    const uint64_t *w = steps + i * 33;
+    const uint32_t kind = (uint32_t)(w[0] >> 32), mask = (uint32_t)w[0];
+    uint64_t res = gal::FAIL;
+    __syncwarp();
+    if (kind == 0) {
+      if ((mask >> lane) & 1u) {  // the step's lanes call together: one team per class
+        void *p = gal::malloc_team(s, w[1 + lane], mask);
+        res = p ? (uint64_t)((char *)p - s->memory) : gal::FAIL;
+      }
+    } else {
+      for (uint32_t l = 0; l < 32; l++) {
+        if (((mask >> l) & 1u) && lane == l) {
+          const uint64_t t = w[1 + l];
+          if (t < i * 32 && out[t] != gal::FAIL) gal::free(s, s->memory + out[t]);
+        }
+        __syncwarp();
+      }
+    }
+    out[i * 32 + lane] = res;
+    __threadfence();
+    __syncwarp();
+  }
+}
+
 __global__ void k_malloc_per_thread(const gal::state *s, const uint64_t *sizes, uint64_t n,
                                     void **out) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -726,6 +757,14 @@ int gal_replay_trace(gal_handle *h, const uint64_t *ops, uint64_t nops, uint64_t
                      uint32_t *out_smid, void *stream) {
   if (!h || !ops || !out_offsets || !out_smid) return GAL_ERR_ARGS;
   k_replay<<<1, 1, 0, (cudaStream_t)stream>>>(h->d_state, ops, nops, out_offsets, out_smid);
+  CUDA_TRY(cudaGetLastError());
+  return GAL_OK;
+}
+
+int gal_replay_warp_trace(gal_handle *h, const uint64_t *steps, uint64_t nsteps,
+                          uint64_t *out_offsets, uint32_t *out_smid, void *stream) {
+  if (!h || (nsteps && (!steps || !out_offsets)) || !out_smid) return GAL_ERR_ARGS;
+  k_replay_warp<<<1, 32, 0, (cudaStream_t)stream>>>(h->d_state, steps, nsteps, out_offsets, out_smid);
   CUDA_TRY(cudaGetLastError());
   return GAL_OK;
 }

@@ -236,6 +236,21 @@ gal_handle *gal_global_host(void);
 int gal_replay_trace(gal_handle *h, const uint64_t *ops, uint64_t nops,
                      uint64_t *out_offsets, uint32_t *out_smid, void *stream);
 
+/* Replay of a trace of warp-wide calls by one warp (thread ids 0-31): the
+ * warp-aggregated slice claim of Gallatin::malloc_slice_allocation
+ * (gallatin.cuh:865-1078) with lanes joining one team.  Step i is 33 words:
+ * steps[33 i] = kind << 32 | lane mask, then one word per lane.  Kind 0: the
+ * masked lanes call malloc together as one set of callers (the device
+ * malloc_team with the step's mask, so the teams do not depend on how the
+ * scheduler regroups diverged lanes), lane l with size steps[33 i + 1 + l];
+ * kind 1: the masked lanes free, one lane at a time in lane order, the
+ * result of earlier call steps[33 i + 1 + l] (an index step * 32 + lane;
+ * failed calls and later indices are skipped).  out_offsets[32 i + l] =
+ * pointer - arena base of a kind-0 result, UINT64_MAX otherwise.  Device
+ * pointers. */
+int gal_replay_warp_trace(gal_handle *h, const uint64_t *steps, uint64_t nsteps,
+                          uint64_t *out_offsets, uint32_t *out_smid, void *stream);
+
 /* One device thread per request: out_ptrs[i] = malloc(sizes[i]) (per-thread
  * global_malloc, global_allocator.cuh:72-76). */
 int gal_malloc_per_thread(gal_handle *h, const uint64_t *sizes, uint64_t n,

@@ -731,12 +731,16 @@ GAL_DEVICE_INLINE char *slice_ptr(const state *s, uint32_t blk, uint64_t idx, ui
 
 // ------------------------------------------------------------------ malloc tiers
 // Gallatin::malloc_slice_allocation (gallatin.cuh:865-1078): warp team per
-// size class, one atomicAdd on the pinned block per team.
-GAL_DEVICE_INLINE void *malloc_slices(const state *s, uint32_t tree, uint32_t count) {
+// size class, one atomicAdd on the pinned block per team.  `pending` holds the
+// lanes that called malloc together and ask for slices (the coalesced group
+// the reference partitions); it shrinks as lanes get their slices, and every
+// warp-wide step of an attempt names it, so a team always holds every caller
+// of its class even when the caller's branches ran as separate groups.
+GAL_DEVICE_INLINE void *malloc_slices(const state *s, uint32_t tree, uint32_t count, uint32_t pending) {
   const uint32_t lane = lane_id();
   const uint64_t tid = thread_linear_id();
   for (int attempt = 0; attempt < SLICE_ATTEMPTS; attempt++) {
-    const uint32_t active = active_lanes();
+    const uint32_t active = pending;
     const uint32_t team = __match_any_sync(active, tree) & team_group(s);
     const int leader = __ffs(team) - 1;
     const int last = 31 - __clz(team);
@@ -748,42 +752,45 @@ GAL_DEVICE_INLINE void *malloc_slices(const state *s, uint32_t tree, uint32_t co
     const uint32_t blk = __shfl_sync(active, seen, leader);
     // teams whose slot was empty retry; the rest carry on with mask `live`
     const uint32_t live = __ballot_sync(active, blk != NOBLK);
-    if (blk == NOBLK) continue;
-
-    uint32_t prefix, total;
-    if (__all_sync(live, count == 1)) {
-      prefix = (uint32_t)__popc(team & lt);
-      total = (uint32_t)__popc(team);
-    } else {  // big slices: counts are powers of two up to one block
-      prefix = 0;
-      total = 0;
-      for (uint32_t c = 1; c <= SLICES_PER_BLOCK; c <<= 1) {
-        uint32_t b = __ballot_sync(live, count == c) & team;
-        prefix += c * (uint32_t)__popc(b & lt);
-        total += c * (uint32_t)__popc(b);
+    void *result = nullptr;
+    bool refill = false;
+    if (blk != NOBLK) {
+      uint32_t prefix, total;
+      if (__all_sync(live, count == 1)) {
+        prefix = (uint32_t)__popc(team & lt);
+        total = (uint32_t)__popc(team);
+      } else {  // big slices: counts are powers of two up to one block
+        prefix = 0;
+        total = 0;
+        for (uint32_t c = 1; c <= SLICES_PER_BLOCK; c <<= 1) {
+          uint32_t b = __ballot_sync(live, count == c) & team;
+          prefix += c * (uint32_t)__popc(b & lt);
+          total += c * (uint32_t)__popc(b);
+        }
+      }
+      unsigned long long old = 0;
+      if ((int)lane == last) old = atomicAdd(&s->mwords[blk], (unsigned long long)total);
+      old = __shfl_sync(live, old, last);
+      const uint64_t alloc = (old & 0xFFFFFFFFull) + prefix;
+      const bool start_valid = alloc <= SLICES_PER_BLOCK - 1;
+      const bool end_valid = alloc + count <= SLICES_PER_BLOCK;
+      const bool should_replace = start_valid && alloc + count > SLICES_PER_BLOCK - 1;
+      uint32_t leftover = start_valid ? (end_valid ? count - 1 : (uint32_t)(SLICES_PER_BLOCK - alloc)) : 0;
+      if (leftover) credit_frees(s, blk, leftover);  // block_correct_frees
+      const uint32_t rep = __ballot_sync(live, should_replace) & team;
+      if (rep && (int)lane == leader) {
+        if (s->use_spares) refill = swap_spare(s, tree, slot, blk, tid);
+        else replace_block(s, tree, slot, blk, tid);
+      }
+      __syncwarp(live);
+      if (start_valid && end_valid) {
+        if ((uint32_t)(old >> 32) == tree) result = slice_ptr(s, blk, alloc, tree);
+        else credit_frees(s, blk, 1);  // Block::check_valid failed: give the slice back
       }
     }
-    unsigned long long old = 0;
-    if ((int)lane == last) old = atomicAdd(&s->mwords[blk], (unsigned long long)total);
-    old = __shfl_sync(live, old, last);
-    const uint64_t alloc = (old & 0xFFFFFFFFull) + prefix;
-    const bool start_valid = alloc <= SLICES_PER_BLOCK - 1;
-    const bool end_valid = alloc + count <= SLICES_PER_BLOCK;
-    const bool should_replace = start_valid && alloc + count > SLICES_PER_BLOCK - 1;
-    uint32_t leftover = start_valid ? (end_valid ? count - 1 : (uint32_t)(SLICES_PER_BLOCK - alloc)) : 0;
-    if (leftover) credit_frees(s, blk, leftover);  // block_correct_frees
-    const uint32_t rep = __ballot_sync(live, should_replace) & team;
-    bool refill = false;
-    if (rep && (int)lane == leader) {
-      if (s->use_spares) refill = swap_spare(s, tree, slot, blk, tid);
-      else replace_block(s, tree, slot, blk, tid);
-    }
-    __syncwarp(live);
+    pending = __ballot_sync(active, result == nullptr);
     if (refill) refill_spare(s, tree, slot, tid);  // the team's other lanes go on
-    if (start_valid && end_valid) {
-      if ((uint32_t)(old >> 32) == tree) return slice_ptr(s, blk, alloc, tree);
-      credit_frees(s, blk, 1);  // Block::check_valid failed: give the slice back
-    }
+    if (result) return result;
   }
   return nullptr;
 }
@@ -830,22 +837,39 @@ GAL_DEVICE_COLD void *malloc_segment_run(const state *s, uint32_t count) {
   return nullptr;
 }
 
-// Gallatin::malloc (gallatin.cuh:1186-1276)
+// the block and segment tiers of Gallatin::malloc (gallatin.cuh:1203-1258)
+GAL_DEVICE_COLD void *malloc_large(const state *s, uint64_t size, int block_tree) {
+  if (block_tree < (int)s->num_trees) return malloc_whole_block(s, (uint32_t)block_tree);
+  return malloc_segment_run(s, (uint32_t)((size - 1) >> s->seg_shift) + 1);
+}
+
+// Gallatin::malloc (gallatin.cuh:1186-1276) called by the lanes in `callers`
+// together: every lane of the mask calls with the same mask (the contract of
+// the *_sync warp intrinsics).  Those that ask for slices form the claim teams,
+// one per size class, and reach malloc_slices on one path (the class and run
+// length are selects, not branches).
+GAL_DEVICE_INLINE void *malloc_team(const state *s, uint64_t size, uint32_t callers) {
+  const uint32_t entered = callers;
+  const int T = (int)s->num_trees;
+  const int bits = ceil_log2(size);
+  const int t = (size >> s->min_shift) == 0 ? 0 : bits - (int)s->min_shift;
+  const int block_tree = bits - (int)(s->min_shift + 12);
+  const bool slices = t < T || block_tree < 0;
+  const uint32_t members = __ballot_sync(entered, slices);
+  if (!slices) return malloc_large(s, size, block_tree);
+  // big slices (4 KiB < size <= 32 KiB by default): runs of the last class
+  const bool big = t >= T;
+  const uint32_t count = 1u << (big ? t - (T - 1) : 0);
+  const uint32_t tree = (uint32_t)(big ? T - 1 : t);
+  return malloc_slices(s, tree, count, members);
+}
+
+// Gallatin::malloc as the reference calls it: the team is the lanes executing
+// the call together (its coalesced_threads(), gallatin.cuh:883).  Which lanes
+// those are after divergence is the scheduler's choice, in either build; a
+// caller that knows its callers names them with malloc_team.
 GAL_DEVICE_INLINE void *malloc(const state *s, uint64_t size) {
-  const uint32_t T = s->num_trees;
-  int bits = ceil_log2(size);
-  int tree = (size >> s->min_shift) == 0 ? 0 : bits - (int)s->min_shift;
-  uint32_t count = 1;
-  if (tree >= (int)T) {
-    int block_tree = bits - (int)(s->min_shift + 12);
-    if (block_tree >= 0) {
-      if (block_tree < (int)T) return malloc_whole_block(s, (uint32_t)block_tree);
-      return malloc_segment_run(s, (uint32_t)((size - 1) >> s->seg_shift) + 1);
-    }
-    count = 1u << (tree - (int)(T - 1));
-    tree = (int)T - 1;
-  }
-  return malloc_slices(s, (uint32_t)tree, count);
+  return malloc_team(s, size, active_lanes());
 }
 
 // multi-segment free (gallatin.cuh:1394-1417, 1283-1302), id reset first

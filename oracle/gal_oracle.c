@@ -709,6 +709,64 @@ static uint64_t malloc_slice(orc_alloc *a, int tree, uint32_t alloc_count, uint3
   return ORC_FAIL;
 }
 
+/* Gallatin::malloc_slice_allocation (gallatin.cuh:865-1078) for one
+ * convergent warp whose lanes in `pending` all ask for slices of `tree`
+ * (counts[l] slices each: 1, or 2-8 for the big-slice sizes of the last tree),
+ * i.e. one labeled_partition team.  Per attempt: the team's lowest lane picks
+ * the slot; the exclusive scan of the counts in lane order gives each lane its
+ * place after the one atomicAdd of the team's total, which the team's last
+ * lane issues (Block::block_malloc_tree_multi_size, block.cuh:245-264); the
+ * leftover slices are credited as one sum (block_correct_frees, :267-281);
+ * the lowest lane replaces the block when some lane crossed slice 4095, with
+ * its own thread id as the sub-tree seed.  Lanes that got a slice leave the
+ * team; the rest form the next attempt's team.  The reference's 10 x 500
+ * attempts are one loop of 5,000: a failing attempt leaves no other state. */
+static void malloc_slice_team(orc_alloc *a, int tree, const uint32_t *counts, uint32_t pending,
+                              uint32_t smid, uint64_t tid0, uint64_t *res) {
+  for (int attempts = 0; attempts < 5000 && pending; attempts++) {
+    int leader = __builtin_ctz(pending);
+    int slot = valid_block_index(a, tree, smid);
+    int32_t blk = a->slots[tree][slot];
+    if (blk == NOBLK) continue;
+    uint32_t merged = a->mc[blk];
+    uint32_t total = 0;
+    for (int l = 0; l < 32; l++)
+      if ((pending >> l) & 1u) total += counts[l];
+    a->mc[blk] = merged + total;
+    uint64_t alloc[32];
+    uint32_t prefix = 0, leftover = 0;
+    int should_replace = 0;
+    for (int l = 0; l < 32; l++) {
+      if (!((pending >> l) & 1u)) continue;
+      uint64_t al = (uint64_t)(merged & 0xFFFFFu) + prefix;
+      uint32_t c = counts[l];
+      prefix += c;
+      int start_valid = al <= 4095, end_valid = al + c <= 4096;
+      if (start_valid && al + c > 4095) should_replace = 1;
+      leftover += start_valid ? (end_valid ? c - 1 : (uint32_t)(4096 - al)) : 0;
+      alloc[l] = end_valid ? al : ORC_FAIL;
+    }
+    if (leftover > 0) {
+      a->fc[blk] += leftover;
+      if ((a->fix & ORC_FIX_LEFTOVER_COMPLETES) && a->fc[blk] == 4096) {
+        a->fc[blk] = 0;
+        free_block(a, blk);
+      }
+    }
+    if (should_replace) replace_block(a, tree, slot, blk, tid0 + (uint64_t)leader);
+    for (int l = 0; l < 32; l++) {
+      if (!((pending >> l) & 1u) || alloc[l] == ORC_FAIL) continue;
+      uint64_t off = alloc[l] + (uint64_t)blk * 4096;
+      if ((merged >> 20) != (uint32_t)tree) { /* Block::check_valid */
+        free_offset(a, off);
+      } else {
+        res[l] = off;
+        pending &= ~(1u << l);
+      }
+    }
+  }
+}
+
 /* Gallatin::malloc_block_allocation (gallatin.cuh:828-861) with
  * Block::malloc_fill_block (block.cuh:288-340) */
 static uint64_t malloc_block(orc_alloc *a, int tree, uint64_t tid) {
@@ -806,6 +864,59 @@ int orc_replay(orc_alloc *a, const uint64_t *ops, uint64_t nops, uint32_t smid, 
     } else {
       out[i] = orc_malloc(a, op, smid, tid);
     }
+  }
+  return 0;
+}
+
+/* A trace of warp-wide calls, replayed by one warp (lanes 0-31 of thread ids
+ * tid0..tid0+31).  Step i is 33 words: word 0 = kind << 32 | lane mask, then
+ * one word per lane.  Kind 0: the masked lanes call malloc together with the
+ * lane's size (all sizes of one step in the same slice class); kind 1: the
+ * masked lanes free, one lane at a time in lane order, the result of the
+ * earlier call whose index (step * 32 + lane) the lane's word holds.  out has
+ * 32 words per step: byte offsets of kind-0 results, ORC_FAIL elsewhere.
+ * A free of a failed call is skipped.  Returns 0, or -1 for a malformed step
+ * (mixed classes, a tier other than slices, a free of a later call). */
+int orc_replay_warp(orc_alloc *a, const uint64_t *steps, uint64_t nsteps, uint32_t smid,
+                    uint64_t tid0, uint64_t *out) {
+  for (uint64_t i = 0; i < nsteps; i++) {
+    const uint64_t *w = steps + i * 33;
+    uint32_t kind = (uint32_t)(w[0] >> 32), mask = (uint32_t)w[0];
+    uint64_t *o = out + i * 32;
+    for (int l = 0; l < 32; l++) o[l] = ORC_FAIL;
+    if (kind == 1) {
+      for (int l = 0; l < 32; l++) {
+        if (!((mask >> l) & 1u)) continue;
+        uint64_t target = w[1 + l];
+        if (target >= i * 32) return -1;
+        if (out[target] != ORC_FAIL) orc_free(a, out[target]);
+      }
+      continue;
+    }
+    if (kind != 0) return -1;
+    int tree = -1;
+    uint32_t counts[32] = {0};
+    for (int l = 0; l < 32; l++) {
+      if (!((mask >> l) & 1u)) continue;
+      uint64_t size = w[1 + l];
+      int t = size < a->min_size ? 0 : first_bit_bigger(size) - a->smallest_bits;
+      uint32_t c = 1;
+      if (t >= a->num_trees) {
+        int block_tree = first_bit_bigger(size) - first_bit_bigger(a->min_size * 4096);
+        if (block_tree >= 0) return -1;
+        c = 1u << (t - (a->num_trees - 1));
+        t = a->num_trees - 1;
+      }
+      if (tree >= 0 && t != tree) return -1;
+      tree = t;
+      counts[l] = c;
+    }
+    if (tree < 0) continue;
+    uint64_t res[32];
+    for (int l = 0; l < 32; l++) res[l] = ORC_FAIL;
+    malloc_slice_team(a, tree, counts, mask, smid, tid0, res);
+    for (int l = 0; l < 32; l++)
+      if (res[l] != ORC_FAIL) o[l] = offset_to_bytes(a, res[l], tree);
   }
   return 0;
 }

@@ -51,6 +51,11 @@ void orc_free(orc_alloc *a, uint64_t byte_offset);
 int orc_replay(orc_alloc *a, const uint64_t *ops, uint64_t nops, uint32_t smid,
                uint64_t tid, uint64_t *out_offsets);
 
+/* replay a trace of warp-wide calls by one warp (encoding as
+ * gal_replay_warp_trace); returns 0, -1 for a malformed step */
+int orc_replay_warp(orc_alloc *a, const uint64_t *steps, uint64_t nsteps, uint32_t smid,
+                    uint64_t tid0, uint64_t *out);
+
 int orc_dims(orc_alloc *a, gal_state_dims *out);
 int orc_export(orc_alloc *a, const gal_state_view *v);
 int orc_import(orc_alloc *a, const gal_state_view *v);

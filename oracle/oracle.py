@@ -45,6 +45,8 @@ def lib():
         L.orc_malloc.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint64]
         L.orc_free.argtypes = [C.c_void_p, C.c_uint64]
         L.orc_replay.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint64, C.c_void_p]
+        L.orc_replay_warp.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint64,
+                                      C.c_void_p]
         L.orc_dims.argtypes = [C.c_void_p, C.c_void_p]
         L.orc_export.argtypes = [C.c_void_p, C.c_void_p]
         L.orc_import.argtypes = [C.c_void_p, C.c_void_p]
@@ -83,6 +85,71 @@ def gen_leftover_trace(slice_size):
     ops = [slice_size] * n + [(1 << 63) | i for i in range(n)] + [2 * slice_size]
     ops.append((1 << 63) | (len(ops) - 1))
     return np.array(ops, dtype=np.uint64)
+
+
+WARP_MALLOC, WARP_FREE = 0, 1
+
+
+def gen_warp_trace(seed, nsteps, malloc_pct=65, tree_weights=(6, 4, 3, 2, 1, 1, 1, 1, 2),
+                   big_pct=30, drain=True, min_size=16):
+    """A trace of warp-wide calls (33 words per step, see orc_replay_warp).
+
+    Malloc steps: a lane mask (the full warp one time in three, else random
+    bits) and one slice class for the whole step, drawn by tree_weights (one
+    weight per class of min_size << t bytes); sizes uniform inside the class
+    (the last class takes big-slice sizes of 2, 4 or 8 slices in big_pct
+    percent of its lanes, mixed with single slices).  Free
+    steps free up to 32 earlier results chosen at random.  With drain, steps
+    freeing everything still live close the trace.  numpy PCG64 seeded with
+    `seed`; the fixtures keep the generated steps themselves."""
+    rng = np.random.default_rng(seed)
+    w = np.asarray(tree_weights, dtype=np.float64)
+    w /= w.sum()
+    steps, live = [], []
+
+    def free_step(targets):
+        row = np.zeros(33, dtype=np.uint64)
+        lanes = np.sort(rng.choice(32, size=len(targets), replace=False))
+        mask = 0
+        for lane, t in zip(lanes, targets):
+            row[1 + lane] = t
+            mask |= 1 << int(lane)
+        row[0] = (WARP_FREE << 32) | mask
+        steps.append(row)
+
+    for _ in range(nsteps):
+        i = len(steps)
+        if live and rng.integers(100) >= malloc_pct:
+            k = int(min(len(live), rng.integers(1, 33)))
+            pick = rng.choice(len(live), size=k, replace=False)
+            targets = [live[j] for j in pick]
+            for j in sorted(pick, reverse=True):
+                live[j] = live[-1]
+                live.pop()
+            free_step(targets)
+            continue
+        mask = 0xFFFFFFFF if rng.integers(3) == 0 else int(rng.integers(1, 1 << 32))
+        t = int(rng.choice(len(w), p=w))
+        row = np.zeros(33, dtype=np.uint64)
+        for lane in range(32):
+            if not (mask >> lane) & 1:
+                continue
+            top = min_size << t
+            if t == len(w) - 1 and rng.integers(100) < big_pct:
+                c = int(rng.choice([2, 4, 8]))
+                size = int(rng.integers(top * c // 2 + 1, top * c + 1))
+            else:
+                lo = 1 if t == 0 else top // 2 + 1
+                size = int(rng.integers(lo, top + 1))
+            row[1 + lane] = size
+            live.append(i * 32 + lane)
+        row[0] = (WARP_MALLOC << 32) | mask
+        steps.append(row)
+    if drain:
+        order = rng.permutation(len(live))
+        for s0 in range(0, len(order), 32):
+            free_step([live[j] for j in order[s0:s0 + 32]])
+    return np.concatenate(steps) if steps else np.zeros(0, dtype=np.uint64)
 
 
 def murmur64a(key, seed):
@@ -131,6 +198,17 @@ class Oracle:
         r = lib().orc_replay(self._h, ops.ctypes.data, len(ops), smid, tid, out.ctypes.data)
         if r != 0:
             raise ValueError("bad trace")
+        return out
+
+    def replay_warp(self, steps, smid=0, tid0=0):
+        """Warp trace (33 words per step) by one modelled warp of thread ids
+        tid0..tid0+31; returns 32 offsets per step."""
+        steps = np.ascontiguousarray(steps, dtype=np.uint64)
+        n = len(steps) // 33
+        out = np.full(n * 32, FAIL, dtype=np.uint64)
+        r = lib().orc_replay_warp(self._h, steps.ctypes.data, n, smid, tid0, out.ctypes.data)
+        if r != 0:
+            raise ValueError("bad warp trace")
         return out
 
     def dims(self):

@@ -221,6 +221,41 @@ extern "C" __global__ void ref_replay(ref_type *a, const uint64_t *ops, uint64_t
   }
 }
 
+// warp trace, one warp (step encoding of gal_replay_warp_trace: 33 words per
+// step, word 0 = kind << 32 | lane mask; kind 0: the masked lanes call malloc
+// together; kind 1: the masked lanes free, one at a time in lane order, the
+// result of call step * 32 + lane named by the lane's word)
+extern "C" __global__ void ref_replay_warp(ref_type *a, const uint64_t *steps, uint64_t nsteps,
+                                           uint64_t *out, uint32_t *out_smid) {
+  if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+  const uint32_t lane = threadIdx.x;
+  if (lane == 0) out_smid[0] = gallatin::utils::get_smid();
+  char *base = a->table->memory;
+  for (uint64_t i = 0; i < nsteps; i++) {
+    const uint64_t *w = steps + i * 33;
+    const uint32_t kind = (uint32_t)(w[0] >> 32), mask = (uint32_t)w[0];
+    uint64_t res = ~0ULL;
+    __syncwarp();
+    if (kind == 0) {
+      if ((mask >> lane) & 1u) {
+        void *p = a->malloc(w[1 + lane]);
+        res = p ? (uint64_t)((char *)p - base) : ~0ULL;
+      }
+    } else {
+      for (uint32_t l = 0; l < 32; l++) {
+        if (((mask >> l) & 1u) && lane == l) {
+          const uint64_t t = w[1 + l];
+          if (t < i * 32 && out[t] != ~0ULL) a->free(base + out[t]);
+        }
+        __syncwarp();
+      }
+    }
+    out[i * 32 + lane] = res;
+    __threadfence();
+    __syncwarp();
+  }
+}
+
 struct export_ptrs {
   uint64_t *seg_tree_words;
   uint64_t *sub_tree_words;

@@ -28,7 +28,7 @@
 static CUcontext g_ctx;
 static CUmodule g_mod;
 static unsigned g_free_grid; /* persistent grid of ref_churn_free: SMs x resident CTAs */
-static CUfunction f_build, f_boot1, f_bootr, f_replay, f_export, f_cmalloc, f_cfree, f_smalloc, f_sfree;
+static CUfunction f_build, f_boot1, f_bootr, f_replay, f_replay_warp, f_export, f_cmalloc, f_cfree, f_smalloc, f_sfree;
 static int g_open = 0;
 
 typedef struct {
@@ -49,6 +49,7 @@ int ref_open(const char *cubin) {
   CK(cuModuleGetFunction(&f_boot1, g_mod, "ref_boot_one_thread"));
   CK(cuModuleGetFunction(&f_bootr, g_mod, "ref_boot_racy"));
   CK(cuModuleGetFunction(&f_replay, g_mod, "ref_replay"));
+  CK(cuModuleGetFunction(&f_replay_warp, g_mod, "ref_replay_warp"));
   CK(cuModuleGetFunction(&f_export, g_mod, "ref_export"));
   CK(cuModuleGetFunction(&f_cmalloc, g_mod, "ref_churn_malloc"));
   CK(cuModuleGetFunction(&f_cfree, g_mod, "ref_churn_free"));
@@ -137,6 +138,27 @@ int ref_replay(void *h, const uint64_t *ops, uint64_t n, uint64_t *out, uint32_t
   CK(cuMemcpyDtoH(out, d_out, n * 8));
   CK(cuMemcpyDtoH(smid, d_smid, 4));
   CK(cuMemFree(d_ops));
+  CK(cuMemFree(d_out));
+  CK(cuMemFree(d_smid));
+  return 0;
+}
+
+/* warp trace: nsteps x 33 words in, nsteps x 32 offsets out, one warp */
+int ref_replay_warp(void *h, const uint64_t *steps, uint64_t nsteps, uint64_t *out, uint32_t *smid) {
+  ref_inst *r = (ref_inst *)h;
+  CUdeviceptr d_steps, d_out, d_smid;
+  CK(cuMemAlloc(&d_steps, nsteps * 33 * 8 + 8));
+  CK(cuMemAlloc(&d_out, nsteps * 32 * 8 + 8));
+  CK(cuMemAlloc(&d_smid, 8));
+  CK(cuMemcpyHtoD(d_steps, steps, nsteps * 33 * 8));
+  CK(cuMemsetD8(d_out, 0xFF, nsteps * 32 * 8));
+  void *args[] = {&r->alloc, &d_steps, &nsteps, &d_out, &d_smid};
+  int e = launch(f_replay_warp, 1, 32, args);
+  if (e) return e;
+  CK(cuCtxSynchronize());
+  CK(cuMemcpyDtoH(out, d_out, nsteps * 32 * 8));
+  CK(cuMemcpyDtoH(smid, d_smid, 4));
+  CK(cuMemFree(d_steps));
   CK(cuMemFree(d_out));
   CK(cuMemFree(d_smid));
   return 0;

@@ -44,6 +44,7 @@ def lib():
         L.ref_create.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.POINTER(C.c_void_p)]
         L.ref_destroy.argtypes = [C.c_void_p]
         L.ref_replay.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]
+        L.ref_replay_warp.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]
         L.ref_export.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.ref_churn.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_int, C.c_int,
                                 C.c_void_p, C.c_void_p]
@@ -83,6 +84,17 @@ class RefGPU:
         r = lib().ref_replay(self._h, ops.ctypes.data, len(ops), out.ctypes.data, smid.ctypes.data)
         if r != 0:
             raise RuntimeError(f"ref_replay failed ({r})")
+        return out, int(smid[0])
+
+    def replay_warp(self, steps):
+        """Warp trace (33 words per step) by one warp; returns (offsets, smid)."""
+        steps = np.ascontiguousarray(steps, dtype=np.uint64)
+        n = len(steps) // 33
+        out = np.full(n * 32, FAIL, dtype=np.uint64)
+        smid = np.zeros(1, dtype=np.uint32)
+        r = lib().ref_replay_warp(self._h, steps.ctypes.data, n, out.ctypes.data, smid.ctypes.data)
+        if r != 0:
+            raise RuntimeError(f"ref_replay_warp failed ({r})")
         return out, int(smid[0])
 
     def export(self, dims: GalStateDims):

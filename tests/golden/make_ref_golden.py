@@ -8,8 +8,12 @@ reference sources are (make -C oracle _ref/ref_harness.cubin):
 For every case it builds the reference's Gallatin<16 MiB, 16, 4096> on the
 device (oracle/ref_harness.cu), records the state after boot, replays a
 serial trace with one device thread and records the offsets it returned
-(pointer - arena base), the SM it ran on, and the final state.  The files
-written here are the fixtures checked by tests/test_oracle_golden.py.
+(pointer - arena base), the SM it ran on, and the final state.  The warp
+cases replay traces of warp-wide calls with one warp instead (the lanes of a
+step join one team of the warp-aggregated slice claim) and go to
+warp_*.npz / warp_index.json.  The files written here are the fixtures
+checked by tests/test_oracle_golden.py.  Names given after the output folder
+select cases; their entries are merged into the index files already there.
 """
 import json
 import os
@@ -22,7 +26,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 sys.path.insert(0, ROOT)
 
 from oracle import refgpu  # noqa: E402
-from oracle.oracle import Oracle, gen_log_trace, gen_serial_trace  # noqa: E402
+from oracle.oracle import Oracle, gen_log_trace, gen_serial_trace, gen_warp_trace  # noqa: E402
 
 GiB = 1 << 30
 
@@ -54,6 +58,54 @@ CASES = [
 ]
 
 
+WARP_CASES = [
+    # name, arena bytes, alloc seed, steps builder (one warp, one-thread boot)
+    ("warp_mixed", 2 * GiB, 42, lambda: gen_warp_trace(5, 3000)),
+    ("warp_small", 2 * GiB, 42, lambda: gen_warp_trace(6, 4000, tree_weights=(8, 4, 0, 0, 0, 0, 0, 0, 0))),
+    ("warp_big", 2 * GiB, 42,
+     lambda: gen_warp_trace(7, 2500, tree_weights=(0, 0, 0, 0, 0, 0, 0, 1, 3), big_pct=50)),
+    ("warp_exhaust", 256 << 20, 42,
+     lambda: gen_warp_trace(8, 800, malloc_pct=85, tree_weights=(0, 0, 0, 0, 0, 0, 1, 1, 4), big_pct=40)),
+]
+
+
+def _merge_index(path, entries):
+    index = json.load(open(path)) if os.path.exists(path) else {}
+    index.update(entries)
+    with open(path, "w") as f:
+        json.dump(index, f, indent=1, sort_keys=True)
+
+
+def warp_cases(out_dir, only):
+    index = {}
+    for name, nbytes, seed, mk in WARP_CASES:
+        if only and name not in only:
+            continue
+        t0 = time.time()
+        steps = mk()
+        rows = steps.reshape(-1, 33)
+        dims = Oracle(nbytes, seed, boot=False).dims()
+        ref = refgpu.RefGPU(nbytes, seed, refgpu.BOOT_ONE_THREAD)
+        boot_state = ref.export(dims)
+        offsets, smid = ref.replay_warp(steps)
+        final_state = ref.export(dims)
+        ref.close()
+        boot_state.to_npz(os.path.join(out_dir, f"{name}.boot.npz"))
+        final_state.to_npz(os.path.join(out_dir, f"{name}.final.npz"), ops=steps, offsets=offsets,
+                           smid=np.array([smid], dtype=np.uint32))
+        mall = (rows[:, 0] >> np.uint64(32)) == 0
+        lanes = (rows[:, 0:1] >> np.arange(32, dtype=np.uint64)) & np.uint64(1)
+        active = (lanes == 1) & mall[:, None]
+        res = offsets.reshape(-1, 32)
+        index[name] = {"arena_bytes": nbytes, "seed": seed, "boot": refgpu.BOOT_ONE_THREAD, "smid": smid,
+                       "steps": int(len(rows)), "mallocs": int(active.sum()),
+                       "failed_mallocs": int((active & (res == np.uint64((1 << 64) - 1))).sum()),
+                       "seconds": round(time.time() - t0, 2)}
+        print(name, index[name], flush=True)
+    if index:
+        _merge_index(os.path.join(out_dir, "warp_index.json"), index)
+
+
 def main():
     out_dir = sys.argv[1] if len(sys.argv) > 1 else os.path.dirname(os.path.abspath(__file__))
     only = set(sys.argv[2:])
@@ -79,8 +131,9 @@ def main():
                        "failed_mallocs": int(((ops < (1 << 63)) & (offsets == (1 << 64) - 1)).sum()),
                        "seconds": round(time.time() - t0, 2)}
         print(name, index[name], flush=True)
-    with open(os.path.join(out_dir, "index.json"), "w") as f:
-        json.dump(index, f, indent=1, sort_keys=True)
+    if index:
+        _merge_index(os.path.join(out_dir, "index.json"), index)
+    warp_cases(out_dir, only)
 
 
 if __name__ == "__main__":

@@ -32,7 +32,7 @@ def test_header_declares_the_boundary():
     names = declared_functions()
     for must in ["gal_create", "gal_destroy", "gal_init", "gal_teardown", "gal_get_stats",
                  "gal_last_error", "gal_device_state", "gal_export_state", "gal_import_state",
-                 "gal_replay_trace", "gal_malloc_per_thread", "gal_free_per_thread",
+                 "gal_replay_trace", "gal_replay_warp_trace", "gal_malloc_per_thread", "gal_free_per_thread",
                  "gal_malloc_batched", "gal_free_batched"]:
         assert must in names
 
@@ -81,4 +81,5 @@ def test_null_arguments_rejected(L):
     assert L.gal_destroy(None) == G._abi.GAL_ERR_ARGS
     assert L.gal_get_stats(None, None) == G._abi.GAL_ERR_ARGS
     assert L.gal_replay_trace(None, None, 0, None, None, None) == G._abi.GAL_ERR_ARGS
+    assert L.gal_replay_warp_trace(None, None, 0, None, None, None) == G._abi.GAL_ERR_ARGS
     assert L.gal_global() is None

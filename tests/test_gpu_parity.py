@@ -15,12 +15,15 @@ import numpy as np
 import pytest
 
 from gallatin_gb300._abi import FAIL, GAL_POLICY_LOWEST, StateView
-from oracle.oracle import PRODUCT_FIXES, Oracle, gen_leftover_trace, gen_log_trace, gen_serial_trace
+from oracle.oracle import (PRODUCT_FIXES, Oracle, gen_leftover_trace, gen_log_trace, gen_serial_trace,
+                           gen_warp_trace)
 
 pytestmark = pytest.mark.gpu
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 INDEX = json.load(open(os.path.join(GOLD, "index.json")))
+_WARP = os.path.join(GOLD, "warp_index.json")
+WARP_INDEX = json.load(open(_WARP)) if os.path.exists(_WARP) else {}
 
 
 @pytest.fixture(scope="module")
@@ -169,6 +172,40 @@ def test_trim_matches_oracle_and_fresh_state(G, mk, nbytes):
         assert sv.diff(o.export()) == []
         assert sv.diff(fresh, fields=["seg_tree_words", "sub_tree_words", "tree_ids", "slots",
                                       "free_counters"]) == []
+        assert g.error_word() == 0
+    finally:
+        g.close()
+
+
+@pytest.mark.parametrize("name", sorted(WARP_INDEX))
+def test_warp_trace_matches_reference_build(G, name):
+    """Warp-wide calls by one warp: the lanes of a step form one team of the
+    warp-aggregated claim; offsets and whole state equal the reference build's."""
+    meta = WARP_INDEX[name]
+    boot, final, steps, offsets, smid = _golden(name)
+    g = G.Gallatin.generate_on_device(meta["arena_bytes"], meta["seed"], smid_override=smid)
+    try:
+        assert g.export().diff(boot) == [], "boot state differs from the reference build"
+        out, _ = g.replay_warp(steps)
+        np.testing.assert_array_equal(out, offsets)
+        assert g.export().diff(final) == [], "final state differs from the reference build"
+        assert g.error_word() == 0
+    finally:
+        g.close()
+
+
+@pytest.mark.parametrize("geom", [(64 << 20, 16, 4096), (64 << 20, 128, 16384), (16 << 20, 128, 4096)])
+def test_warp_traces_on_other_geometries_match_oracle(G, geom):
+    seg, mn, mx = geom
+    trees = (mx // mn).bit_length()
+    steps = gen_warp_trace(909, 1500, tree_weights=(3,) + (1,) * (trees - 2) + (3,), big_pct=40,
+                           min_size=mn)
+    g = G.Gallatin.generate_on_device(4 << 30, 3, bytes_per_segment=seg, min_size=mn, max_size=mx)
+    try:
+        out, smid = g.replay_warp(steps)
+        o = Oracle(4 << 30, 3, bytes_per_segment=seg, min_size=mn, max_size=mx, fixes=PRODUCT_FIXES)
+        np.testing.assert_array_equal(out, o.replay_warp(steps, smid=smid))
+        assert g.export().diff(o.export()) == []
         assert g.error_word() == 0
     finally:
         g.close()

@@ -3,7 +3,9 @@
 tests/golden/*.npz were written by tests/golden/make_ref_golden.py, which ran
 the reference allocator (compiled from its sources) on a GB300: state after
 boot, the offset every malloc of a serial trace returned, the SM the trace ran
-on, and the state after the trace.  The oracle in pure-reference mode
+on, and the state after the trace.  The warp_* fixtures replay traces of
+warp-wide calls with one warp instead: the lanes of a step form one team of
+the warp-aggregated slice claim.  The oracle in pure-reference mode
 (fixes=0) must reproduce all of it bit for bit.
 """
 import json
@@ -17,6 +19,8 @@ from oracle.oracle import PRODUCT_FIXES, Oracle
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 INDEX = json.load(open(os.path.join(GOLD, "index.json")))
+_WARP = os.path.join(GOLD, "warp_index.json")
+WARP_INDEX = json.load(open(_WARP)) if os.path.exists(_WARP) else {}
 
 
 def load_case(name):
@@ -69,3 +73,19 @@ def test_golden_serial_trace_has_no_failures():
     _, _, ops, offsets, _ = load_case("cfg1_serial")
     m = ops < (1 << 63)
     assert m.sum() == 2456 and not (offsets[m] == FAIL).any()
+
+
+@pytest.mark.parametrize("name", sorted(WARP_INDEX))
+def test_oracle_warp_teams_match_reference_build(name):
+    """One warp of the reference build: every lane's offset (lane-order scan
+    of the team, one atomic per team, block replacement by the team's lowest
+    lane with its own thread id) and the whole state after the trace."""
+    meta = WARP_INDEX[name]
+    boot, final, steps, offsets, smid = load_case(name)
+    o = Oracle(meta["arena_bytes"], meta["seed"], fixes=0)
+    assert o.export().diff(boot) == []
+    out = o.replay_warp(steps, smid=smid)
+    np.testing.assert_array_equal(out, offsets)
+    assert o.export().diff(final) == []
+    p = Oracle(meta["arena_bytes"], meta["seed"], fixes=PRODUCT_FIXES)
+    np.testing.assert_array_equal(p.replay_warp(steps, smid=smid), offsets)
