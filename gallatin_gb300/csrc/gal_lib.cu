@@ -499,6 +499,21 @@ int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot
   return GAL_OK;
 }
 
+// makes h the process-wide instance unless another thread installed one while
+// h was being built (the check before building is only a fast path)
+int install_global(gal_handle **slot, gal_handle *h) {
+  {
+    std::lock_guard<std::mutex> g(g_mu);
+    if (!*slot) {
+      *slot = h;
+      return GAL_OK;
+    }
+    g_by_state.erase(h->d_state);
+  }
+  free_handle(h);
+  return GAL_ERR_STATE;
+}
+
 int push_state(gal_handle *h) {
   CUDA_TRY(cudaMemcpy(h->d_state, &h->st, sizeof(h->st), cudaMemcpyHostToDevice));
   return GAL_OK;
@@ -570,7 +585,8 @@ int gal_get_stats(gal_handle *h, gal_stats *out) {
   gal_stats *d = nullptr;
   CUDA_TRY(cudaMalloc(&d, sizeof(gal_stats)));
   k_stats<<<1, 1024>>>(h->d_state, d);
-  cudaError_t e = cudaMemcpy(out, d, sizeof(gal_stats), cudaMemcpyDeviceToHost);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(out, d, sizeof(gal_stats), cudaMemcpyDeviceToHost);
   cudaFree(d);
   if (e != cudaSuccess) return GAL_ERR_CUDA;
   out->metadata_bytes = h->meta_bytes;
@@ -701,9 +717,7 @@ int gal_init(uint64_t num_bytes, uint64_t seed, const gal_config *cfg) {
   gal_handle *h = nullptr;
   int rc = gal_create(num_bytes, seed, cfg, &h);
   if (rc) return rc;
-  std::lock_guard<std::mutex> g(g_mu);
-  g_global = h;
-  return GAL_OK;
+  return install_global(&g_global, h);
 }
 
 int gal_teardown(void) {
@@ -733,9 +747,7 @@ int gal_init_host(uint64_t num_bytes, uint64_t seed, const gal_config *cfg) {
   gal_handle *h = nullptr;
   int rc = gal_create(num_bytes, seed, &c, &h);
   if (rc) return rc;
-  std::lock_guard<std::mutex> g(g_mu);
-  g_global_host = h;
-  return GAL_OK;
+  return install_global(&g_global_host, h);
 }
 
 int gal_teardown_host(void) {

@@ -83,3 +83,32 @@ def test_poison_detects_padding_writes(D):
     out = np.zeros(5, dtype=np.uint64)
     assert _fn(D, "dropin_poison_test", 3)(2 << 30, 1 << 14, 100, out.ctypes.data) == 0
     assert out.tolist() == [0, 0, 0, 0, 0]
+
+
+def test_concurrent_global_init_installs_one_instance():
+    """Host threads racing init_global_allocator: one instance is installed,
+    the others get GAL_ERR_STATE and leave nothing behind."""
+    import threading
+
+    import gallatin_gb300 as G
+    L = G.lib()
+    assert L.gal_global() is None
+    rcs = []
+    lock = threading.Lock()
+
+    def init():
+        rc = L.gal_init(1 << 30, 42, None)
+        with lock:
+            rcs.append(rc)
+
+    threads = [threading.Thread(target=init) for _ in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    try:
+        assert sorted(rcs) == [G._abi.GAL_OK] + [G._abi.GAL_ERR_STATE] * 3
+        assert L.gal_global() is not None
+    finally:
+        assert L.gal_teardown() == G._abi.GAL_OK
+    assert L.gal_global() is None
