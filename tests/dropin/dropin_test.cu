@@ -414,3 +414,60 @@ extern "C" int dropin_divergent_test(uint64_t num_bytes, uint64_t n, int rounds,
   out[3] = err;
   return e == cudaSuccess ? 0 : 1;
 }
+
+// The reference's pointer churn (tests/src/global_churn.cu:184-245): every
+// thread loops: malloc of a hashed size, exchange its id into the first word
+// (the old word must be 0: the arena starts zeroed and every user clears the
+// word before freeing), exchange 0 back (the word must still hold the id),
+// free.  A shared allocation shows up as a non-zero old word or a changed id.
+// Sizes span [min_size, max_size) here; the reference's host passes the two
+// swapped (global_churn.cu:295 vs :185), so every request there was max_size.
+__device__ uint64_t churn_mix(uint64_t x) {  // splitmix64 finaliser
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+__global__ void pointer_churn(uint64_t n, int rounds, uint64_t min_size, uint64_t max_size,
+                              unsigned long long *c) {
+  const uint64_t tid = threadIdx.x + (uint64_t)blockIdx.x * blockDim.x;
+  if (tid >= n) return;
+  const unsigned long long me = tid + 1;
+  uint64_t h = tid;
+  for (int i = 0; i < rounds; i++) {
+    h = churn_mix(h ^ (uint64_t)i);
+    const uint64_t size = min_size + h % (max_size - min_size);
+    unsigned long long *p = (unsigned long long *)global_malloc(size);
+    for (int retry = 0; p == nullptr && retry < 10; retry++) p = (unsigned long long *)global_malloc(size);
+    if (p == nullptr) {
+      atomicAdd(&c[0], 1ull);
+      continue;
+    }
+    if (atomicExch(p, me) != 0ull) atomicAdd(&c[1], 1ull);
+    if (atomicExch(p, 0ull) != me) atomicAdd(&c[2], 1ull);
+    global_free(p);
+  }
+}
+
+extern "C" int dropin_churn_test(uint64_t num_bytes, uint64_t n, int rounds, uint64_t min_size,
+                                 uint64_t max_size, uint64_t *out) {
+  if (max_size <= min_size || min_size < 8) return 3;
+  init_global_allocator(num_bytes, 111, false);
+  unsigned long long *c = nullptr;
+  cudaMalloc(&c, 4 * sizeof(unsigned long long));
+  cudaMemset(c, 0, 4 * sizeof(unsigned long long));
+  pointer_churn<<<(unsigned)((n + 255) / 256), 256>>>(n, rounds, min_size, max_size, c);
+  cudaError_t e = cudaDeviceSynchronize();
+  unsigned long long h[4] = {0, 0, 0, 0};
+  cudaMemcpy(h, c, sizeof(h), cudaMemcpyDeviceToHost);
+  uint32_t err = 0;
+  gal_last_error(gal_global(), &err);
+  cudaFree(c);
+  free_global_allocator();
+  out[0] = h[0];  // requests that failed 11 times
+  out[1] = h[1];  // allocation already held another thread's id
+  out[2] = h[2];  // id changed while held
+  out[3] = err;
+  return e == cudaSuccess ? 0 : 1;
+}

@@ -112,3 +112,17 @@ def test_concurrent_global_init_installs_one_instance():
     finally:
         assert L.gal_teardown() == G._abi.GAL_OK
     assert L.gal_global() is None
+
+
+@pytest.mark.parametrize("n,rounds,lo,hi,arena", [
+    (1 << 20, 16, 16, 4096, 8 << 30),        # slices of every class
+    (1 << 16, 16, 16, 64 << 10, 8 << 30),    # plus big slices and whole blocks
+], ids=["slices", "blocks"])
+def test_pointer_churn_exchange_check(D, n, rounds, lo, hi, arena):
+    """The reference's global_churn: malloc, exchange the id in and out, free,
+    in a loop per thread; no allocation is ever shared and none fails."""
+    D.dropin_churn_test.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.c_uint64, C.c_uint64, C.c_void_p]
+    D.dropin_churn_test.restype = C.c_int
+    out = np.zeros(4, dtype=np.uint64)
+    assert D.dropin_churn_test(arena, n, rounds, lo, hi, out.ctypes.data) == 0
+    assert out.tolist() == [0, 0, 0, 0]
