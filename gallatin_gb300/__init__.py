@@ -380,7 +380,7 @@ def atomic_peak():
 # ---- process-global instance (global_allocator.cuh:41-97) ----
 def init_global_allocator(num_bytes, seed, print_info=True, running_calloc=False, **cfg):
     if running_calloc:
-        raise GalError("calloc mode (dynamic parallelism) is not provided")
+        cfg["zero_fill"] = 1  # calloc mode: every allocation handed out zeroed
     config = default_config(**cfg)
     _check(lib().gal_init(num_bytes, seed, C.byref(config)), "gal_init")
     if print_info:

@@ -48,6 +48,7 @@ class GalConfig(C.Structure):
         ("team_width", C.c_uint32),
         ("arena_kind", C.c_uint32),
         ("spare_blocks", C.c_uint32),
+        ("zero_fill", C.c_uint32),
     ]
 
 

@@ -197,7 +197,8 @@ __device__ __forceinline__ void cta_malloc_n(const state *s, const uint64_t (&si
         r -= len;
       }
     }
-    if (fallback) p = gal::malloc(s, size[k]);
+    if (fallback) p = gal::malloc(s, size[k]);  // clears its own bytes in calloc mode
+    else if (p && s->zero_fill) zero_fill(p, size[k]);
     out[k] = p;
   }
   cta_sync(sm);

@@ -349,7 +349,7 @@ int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot
   if (cfg.subtree_policy > GAL_POLICY_LOWEST) return GAL_ERR_ARGS;
   if (cfg.team_width > 32 || (cfg.team_width & (cfg.team_width - 1))) return GAL_ERR_ARGS;
   if (cfg.arena_kind > GAL_ARENA_MANAGED) return GAL_ERR_ARGS;
-  if (cfg.spare_blocks > 1) return GAL_ERR_ARGS;
+  if (cfg.spare_blocks > 1 || cfg.zero_fill > 1) return GAL_ERR_ARGS;
   const uint32_t T = log2u(cfg.max_size) - log2u(cfg.min_size) + 1;
   const uint64_t S = num_bytes / cfg.bytes_per_segment;
   if (T > GAL_MAX_TREES || S == 0 || S + T + 1 >= 0xFFFF) return GAL_ERR_ARGS;
@@ -375,6 +375,7 @@ int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot
   st.gather_unlocked_below = cfg.gather_unlocked_below;
   st.team_width = cfg.team_width ? cfg.team_width : 32;
   st.use_spares = cfg.spare_blocks ? 1u : 0u;
+  st.zero_fill = cfg.zero_fill;
   // pinned slots: first, halving per tree, floored (shared_block_storage.cuh:260-267);
   // pinned_slots_first == 0 asks for one slot per SM in every size class
   if (cfg.pinned_slots_first == 0) {
@@ -546,6 +547,7 @@ int gal_config_default(gal_config *cfg) {
   cfg->team_width = 32;
   cfg->arena_kind = GAL_ARENA_DEVICE;
   cfg->spare_blocks = 0;
+  cfg->zero_fill = 0;
   return GAL_OK;
 }
 

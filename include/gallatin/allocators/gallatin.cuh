@@ -63,12 +63,9 @@ struct Gallatin {
 
   static __host__ my_type *generate_with_arena(uint64_t max_bytes, uint64_t seed, bool print_info,
                                                bool running_calloc, uint32_t arena_kind) {
-    if (running_calloc) {
-      fprintf(stderr, "Gallatin: calloc mode (dynamic parallelism) is not provided\n");
-      return nullptr;
-    }
     gal_config cfg = config();
     cfg.arena_kind = arena_kind;
+    cfg.zero_fill = running_calloc ? 1u : 0u;  // calloc mode: allocations handed out zeroed
     gal_handle *h = nullptr;
     int rc = gal_create(max_bytes, seed, &cfg, &h);
     if (rc != GAL_OK) {

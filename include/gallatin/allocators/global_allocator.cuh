@@ -33,11 +33,8 @@ static __device__ global_allocator_type *global_host_gallatin;
 
 __host__ inline void init_global_allocator(uint64_t num_bytes, uint64_t seed, bool print_info = true,
                                            bool running_calloc = false) {
-  if (running_calloc) {
-    fprintf(stderr, "Gallatin: calloc mode (dynamic parallelism) is not provided\n");
-    return;
-  }
   gal_config cfg = global_allocator_type::config();
+  cfg.zero_fill = running_calloc ? 1u : 0u;  // calloc mode: allocations handed out zeroed
   int rc = gal_init(num_bytes, seed, &cfg);
   if (rc != GAL_OK) {
     fprintf(stderr, "Gallatin: init_global_allocator failed with status %d\n", rc);
@@ -73,11 +70,8 @@ __host__ inline void print_global_stats() {
 
 __host__ inline void init_global_allocator_host(uint64_t num_bytes, uint64_t seed, bool print_info = true,
                                                 bool running_calloc = false) {
-  if (running_calloc) {
-    fprintf(stderr, "Gallatin: calloc mode (dynamic parallelism) is not provided\n");
-    return;
-  }
   gal_config cfg = global_allocator_type::config();
+  cfg.zero_fill = running_calloc ? 1u : 0u;  // calloc mode: allocations handed out zeroed
   int rc = gal_init_host(num_bytes, seed, &cfg);
   if (rc != GAL_OK) {
     fprintf(stderr, "Gallatin: init_global_allocator_host failed with status %d\n", rc);

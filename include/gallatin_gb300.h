@@ -88,6 +88,13 @@ typedef struct gal_config {
                                    Costs one block per slot held in reserve;
                                    serial offsets then differ from the
                                    reference's.  0 = the reference's behaviour. */
+  uint32_t zero_fill;           /* 1: calloc mode (the reference's running_calloc):
+                                   the requested bytes of every allocation are
+                                   zero when handed out.  The reference keeps
+                                   returned blocks and segment runs zero by
+                                   clearing them in child kernels (dynamic
+                                   parallelism); here the allocating thread
+                                   clears its own bytes.  Default 0.            */
 } gal_config;
 
 /* Arena backing (gal_config.arena_kind). */

@@ -77,6 +77,7 @@ struct state {
   uint32_t gather_unlocked_below;  // see gal_config
   uint32_t team_width;             // see gal_config (1..32, a power of two)
   uint32_t use_spares;             // see gal_config.spare_blocks
+  uint32_t zero_fill;              // see gal_config.zero_fill
   uint32_t slot_base[GAL_MAX_TREES];
   uint32_t slot_count[GAL_MAX_TREES];
   veb_shape veb;
@@ -837,6 +838,20 @@ GAL_DEVICE_COLD void *malloc_segment_run(const state *s, uint32_t count) {
   return nullptr;
 }
 
+// calloc mode (gal_config.zero_fill): the requested bytes, rounded up to 16,
+// are cleared by the allocating thread.  Every allocation starts on a 16-byte
+// boundary and covers at least its request rounded up to 16 (slices are at
+// least 16 B), so the stores stay inside it.
+GAL_DEVICE_COLD void zero_fill(void *p, uint64_t size) {
+  uint4 *q = (uint4 *)p;
+  const uint64_t n = size ? (size + 15) >> 4 : 1;
+  for (uint64_t i = 0; i < n; i++) q[i] = make_uint4(0u, 0u, 0u, 0u);
+}
+GAL_DEVICE_INLINE void *handed_out(const state *s, void *p, uint64_t size) {
+  if (p && s->zero_fill) zero_fill(p, size);
+  return p;
+}
+
 // the block and segment tiers of Gallatin::malloc (gallatin.cuh:1203-1258)
 GAL_DEVICE_COLD void *malloc_large(const state *s, uint64_t size, int block_tree) {
   if (block_tree < (int)s->num_trees) return malloc_whole_block(s, (uint32_t)block_tree);
@@ -856,12 +871,12 @@ GAL_DEVICE_INLINE void *malloc_team(const state *s, uint64_t size, uint32_t call
   const int block_tree = bits - (int)(s->min_shift + 12);
   const bool slices = t < T || block_tree < 0;
   const uint32_t members = __ballot_sync(entered, slices);
-  if (!slices) return malloc_large(s, size, block_tree);
+  if (!slices) return handed_out(s, malloc_large(s, size, block_tree), size);
   // big slices (4 KiB < size <= 32 KiB by default): runs of the last class
   const bool big = t >= T;
   const uint32_t count = 1u << (big ? t - (T - 1) : 0);
   const uint32_t tree = (uint32_t)(big ? T - 1 : t);
-  return malloc_slices(s, tree, count, members);
+  return handed_out(s, malloc_slices(s, tree, count, members), size);
 }
 
 // Gallatin::malloc as the reference calls it: the team is the lanes executing

@@ -471,3 +471,59 @@ extern "C" int dropin_churn_test(uint64_t num_bytes, uint64_t n, int rounds, uin
   out[3] = err;
   return e == cudaSuccess ? 0 : 1;
 }
+
+// calloc mode (init_global_allocator(..., running_calloc = true)): every
+// allocation reads zero over its requested bytes, also when its memory was
+// written by an earlier allocation and came back through a free.  Half the
+// requests are whole blocks (32-64 KiB), which a free returns to their
+// segment for the next round to reuse; the rest are slices.
+__global__ void calloc_round(uint64_t n, int round, unsigned char **bits, unsigned long long *c) {
+  const uint64_t tid = threadIdx.x + (uint64_t)blockIdx.x * blockDim.x;
+  if (tid >= n) return;
+  const uint64_t h = churn_mix(tid * 0x100000001B3ull + (uint64_t)round);
+  const uint64_t size = (h & 1) ? 32769 + (h >> 1) % 32768 : 16 + (h >> 1) % 4081;
+  unsigned char *p = (unsigned char *)global_malloc(size);
+  bits[tid] = p;
+  if (p == nullptr) {
+    atomicAdd(&c[0], 1ull);
+    return;
+  }
+  bool dirty = false;
+  const uint32_t *w = (const uint32_t *)p;  // allocations start 16-byte aligned
+  for (uint64_t i = 0; i < size / 4; i++) dirty |= w[i] != 0u;
+  for (uint64_t i = size & ~3ull; i < size; i++) dirty |= p[i] != 0;
+  if (dirty) atomicAdd(&c[1], 1ull);
+  for (uint64_t i = 0; i < size; i++) p[i] = 0xA5;  // leave the memory dirty
+}
+
+__global__ void calloc_free(uint64_t n, unsigned char **bits) {
+  const uint64_t tid = threadIdx.x + (uint64_t)blockIdx.x * blockDim.x;
+  if (tid < n && bits[tid]) global_free(bits[tid]);
+}
+
+extern "C" int dropin_calloc_test(uint64_t num_bytes, uint64_t n, int rounds, int calloc_mode, uint64_t *out) {
+  init_global_allocator(num_bytes, 42, false, calloc_mode != 0);
+  if (!gal_global()) return 2;
+  unsigned char **bits = nullptr;
+  unsigned long long *c = nullptr;
+  cudaMalloc(&bits, n * sizeof(unsigned char *));
+  cudaMalloc(&c, 4 * sizeof(unsigned long long));
+  cudaMemset(c, 0, 4 * sizeof(unsigned long long));
+  for (int r = 0; r < rounds; r++) {
+    calloc_round<<<(unsigned)((n + 255) / 256), 256>>>(n, r, bits, c);
+    calloc_free<<<(unsigned)((n + 255) / 256), 256>>>(n, bits);
+  }
+  cudaError_t e = cudaDeviceSynchronize();
+  unsigned long long h[4] = {0, 0, 0, 0};
+  cudaMemcpy(h, c, sizeof(h), cudaMemcpyDeviceToHost);
+  uint32_t err = 0;
+  gal_last_error(gal_global(), &err);
+  cudaFree(bits);
+  cudaFree(c);
+  free_global_allocator();
+  out[0] = h[0];  // failed requests
+  out[1] = h[1];  // allocations that did not read zero
+  out[2] = 0;
+  out[3] = err;
+  return e == cudaSuccess ? 0 : 1;
+}

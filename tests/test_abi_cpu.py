@@ -61,6 +61,7 @@ def test_default_config_is_reference_geometry(L):
     dict(team_width=64),                       # wider than a warp
     dict(arena_kind=3),                        # device, host or managed only
     dict(spare_blocks=2),                      # off or on
+    dict(zero_fill=2),                         # off or on
 ])
 def test_invalid_config_rejected_before_device_use(L, kw):
     import gallatin_gb300 as G

@@ -126,3 +126,19 @@ def test_pointer_churn_exchange_check(D, n, rounds, lo, hi, arena):
     out = np.zeros(4, dtype=np.uint64)
     assert D.dropin_churn_test(arena, n, rounds, lo, hi, out.ctypes.data) == 0
     assert out.tolist() == [0, 0, 0, 0]
+
+
+@pytest.mark.parametrize("calloc_mode", [1, 0], ids=["calloc", "plain"])
+def test_calloc_mode_hands_out_zeroed_memory(D, calloc_mode):
+    """running_calloc = true: every allocation reads zero, also on memory that
+    earlier rounds wrote and freed.  Without it the same rounds do see that
+    memory again (the check detects dirt), the reference's plain behaviour."""
+    D.dropin_calloc_test.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.c_int, C.c_void_p]
+    D.dropin_calloc_test.restype = C.c_int
+    out = np.zeros(4, dtype=np.uint64)
+    assert D.dropin_calloc_test(4 << 30, 1 << 14, 6, calloc_mode, out.ctypes.data) == 0
+    assert out[0] == 0 and out[3] == 0
+    if calloc_mode:
+        assert out[1] == 0
+    else:
+        assert out[1] > 0
