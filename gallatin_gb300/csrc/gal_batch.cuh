@@ -149,6 +149,10 @@ __device__ __forceinline__ void cta_workers_done(cta_claim_smem &sm) {
   if (threadIdx.x == 0) *(volatile uint32_t *)&sm.stop = 1u;
 }
 
+// Requests the CTA claim does not serve take the per-thread path, out of line
+// so that it does not weigh on the claim loop's registers.
+GAL_DEVICE_COLD void *malloc_fallback(const state *s, uint64_t size) { return gal::malloc(s, size); }
+
 // Serves K requests per thread (request k of every thread of the CTA ranked
 // together, one claim per class for all of them); out[k] = nullptr where
 // has_request[k] is false.  More requests per call amortise the claim round
@@ -197,7 +201,7 @@ __device__ __forceinline__ void cta_malloc_n(const state *s, const uint64_t (&si
         r -= len;
       }
     }
-    if (fallback) p = gal::malloc(s, size[k]);  // clears its own bytes in calloc mode
+    if (fallback) p = malloc_fallback(s, size[k]);  // clears its own bytes in calloc mode
     else if (p && s->zero_fill) zero_fill(p, size[k]);
     out[k] = p;
   }
