@@ -250,6 +250,33 @@ def test_churn_rounds_must_align(G):
         g.close()
 
 
+def test_batch_larger_than_the_arena(G, torch):
+    """gal_malloc_batched asked for more than the arena holds: the requests
+    it cannot serve come back as nullptr, the rest are disjoint, and freeing
+    them gives the segments back."""
+    g = G.Gallatin.generate_on_device(512 << 20, 42)
+    try:
+        n = 300_000
+        d_sizes = torch.full((n,), 4096, dtype=torch.int64, device="cuda")
+        d_sizes[::3] = 64
+        d_ptrs = torch.zeros(n, dtype=torch.int64, device="cuda")
+        g.malloc_batched(d_sizes, d_ptrs)
+        torch.cuda.synchronize()
+        ptrs = d_ptrs.cpu().numpy()
+        sizes = d_sizes.cpu().numpy()
+        ok = ptrs != 0
+        assert 0 < ok.sum() < n
+        _check_no_overlap(ptrs[ok], sizes[ok], g.arena_base)
+        assert g.error_word() == 0, g.error_info()
+        g.free_batched(d_ptrs)
+        torch.cuda.synchronize()
+        assert g.stats().free_segments > 0
+        assert g.error_word() == 0, g.error_info()
+        assert (g.export().free_counters <= 4096).all()
+    finally:
+        g.close()
+
+
 def test_exhaustion_returns_null_then_recovers(G, torch):
     """Tiny arena: 4 KiB class runs dry, frees give whole segments back, and
     whole-block requests are served again."""
