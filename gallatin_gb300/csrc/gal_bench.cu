@@ -1,4 +1,4 @@
-// gal_bench.cu — workload drivers used by bench.py and the GPU tests:
+// gal_bench.cu — workload kernels used by bench.py and the GPU tests:
 //   * mixed-size churn (16 B–4 KiB, 50% random frees per round, uint32
 //     payload written and checked), plain per-thread or CTA-batched, stream
 //     launches or one captured CUDA graph per step;

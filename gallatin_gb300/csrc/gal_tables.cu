@@ -1,5 +1,5 @@
 // gal_tables.cu — batched uneven instances: many chained hash tables served by
-// the device allocator in one launch per phase (the driver of the reference's
+// the device allocator in one launch per phase (the workload of the reference's
 // data_structs/chaining_table.cuh:114-327, which has no delete; the table here
 // is this library's own).
 //

@@ -195,8 +195,8 @@ int gal_clear_error(gal_handle *h);
 /* First recorded error: out4 = {site, value a, value b, recorded flag}. */
 int gal_error_info(gal_handle *h, uint64_t *out4);
 
-/* State view export/import (no reference counterpart: test and drain-check
- * support, SURVEY-style "snapshot"). */
+/* State view export/import (no reference counterpart: a snapshot of every
+ * metadata array, for parity tests and drain checks). */
 int gal_state_dims_get(gal_handle *h, gal_state_dims *out);
 int gal_export_state(gal_handle *h, const gal_state_view *view);
 int gal_import_state(gal_handle *h, const gal_state_view *view);
