@@ -1,7 +1,7 @@
 /*
  * gal_oracle.c — single-threaded CPU restatement of the reference allocator.
  *
- * TEST INFRASTRUCTURE ONLY (the checker).  Nothing in the product links it.
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the product links it.
  *
  * Every function names the reference code it restates (paths inside the
  * chillenzer/gallatin project, include/gallatin/allocators/).  The model runs
