@@ -527,7 +527,9 @@ def main():
                 "d2h_bytes_per_step": int(eres.d2h_bytes),
                 "path": "gal_malloc_batched / gal_free_batched_n C ABI with user stamp and selection "
                         "kernels; each round's sizes copied H2D from pinned host memory, counters "
-                        "read back; the step captured once as a CUDA graph (two streams)"},
+                        "read back; the selection of older rounds' slots overlaps the previous "
+                        "round's allocator calls on its own stream; the step captured once as a "
+                        "CUDA graph (three streams)"},
         "latency": latency,
         "gpu_launches": int(res.malloc_launches + res.free_launches),
         "clocks": clk.summary(),

@@ -208,8 +208,8 @@ __device__ __forceinline__ void churn_free_warps(Alloc *a, void **ptrs, uint32_t
 // The same selection, but the selected pointers are appended to freelist
 // (*count entries so far; one atomicAdd per warp and chunk) for a batched
 // free call to serve; payloads are checked here.
-__device__ __forceinline__ void churn_select_warps(void **ptrs, uint32_t *live_bits, uint64_t nslots,
-                                                   uint32_t round, uint32_t seed, bool all,
+__device__ __forceinline__ void churn_select_warps(void **ptrs, uint32_t *live_bits, uint64_t lo_slots,
+                                                   uint64_t nslots, uint32_t round, uint32_t seed, bool all,
                                                    unsigned long long *stats, uint16_t *list,
                                                    void **freelist, unsigned long long *count) {
   const uint32_t lane = threadIdx.x & 31u;
@@ -217,7 +217,7 @@ __device__ __forceinline__ void churn_select_warps(void **ptrs, uint32_t *live_b
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   const uint64_t words = nslots >> 5;
   uint32_t nbad = 0, ngo = 0;
-  for (uint64_t w0 = warp * WARP_WORDS; w0 < words; w0 += nwarps * WARP_WORDS) {
+  for (uint64_t w0 = (lo_slots >> 5) + warp * WARP_WORDS; w0 < words; w0 += nwarps * WARP_WORDS) {
     const uint32_t total = list_selected(live_bits, words, w0, round, seed, all, list);
     if (total == 0) continue;  // warp-uniform
     unsigned long long base = 0;

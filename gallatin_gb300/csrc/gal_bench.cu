@@ -162,10 +162,10 @@ __global__ void k_stamp_payload(void **ptrs, uint32_t *live, uint64_t base, uint
 // and checks their payloads; persistent grid, one warp per 1,024 slots.
 __global__ void __launch_bounds__(FREE_BT)
     k_select_free_list(void **ptrs, uint32_t *live, void **freelist, unsigned long long *count,
-                       uint64_t nslots, uint32_t round, uint32_t seed, int all,
+                       uint64_t lo, uint64_t nslots, uint32_t round, uint32_t seed, int all,
                        unsigned long long *stats) {
   __shared__ uint16_t lists[FREE_BT / 32][galwl::WARP_SLOTS];
-  galwl::churn_select_warps(ptrs, live, nslots, round, seed, all != 0, stats, lists[threadIdx.x >> 5],
+  galwl::churn_select_warps(ptrs, live, lo, nslots, round, seed, all != 0, stats, lists[threadIdx.x >> 5],
                             freelist, count);
 }
 
@@ -479,8 +479,13 @@ done:
  * gal_malloc_batched; a user kernel stamps the payloads; frees are selected by
  * a user kernel that compacts them into a list whose length stays on the
  * device, served by gal_free_batched_n; the step's counters are read back.
- * use_graph: the step (both streams, copies included) is captured once as a
- * CUDA graph, as a user replaying the same step would. */
+ * The selection runs on a third stream in two parts: the slots of the older
+ * rounds as soon as the previous selection is done (overlapping the previous
+ * round's free, malloc and stamp), the slots of the round just stamped after
+ * its stamp; the two free lists alternate between rounds.  Each round still
+ * frees before it allocates.  use_graph: the step (all three streams, copies
+ * included) is captured once as a CUDA graph, as a user replaying the same
+ * step would. */
 int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t threads_per_round,
                         uint32_t rounds, uint32_t seed, int warmup, int steps, float *step_ms,
                         gal_churn_result *res, int use_graph) {
@@ -488,13 +493,13 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
   if (threads_per_round % galwl::SLOT_ALIGN) return GAL_ERR_ARGS;
   int rc = GAL_OK;
   const uint64_t N = threads_per_round, nslots = N * rounds;
-  void **ptrs = nullptr, **freelist = nullptr;
+  void **ptrs = nullptr, **freelist[2] = {nullptr, nullptr};
   uint32_t *live = nullptr;
   uint64_t *d_sizes[2] = {nullptr, nullptr};
-  unsigned long long *stats = nullptr, *count = nullptr, *hst = nullptr;  // hst: pinned host
-  cudaStream_t st = nullptr, cp = nullptr;
+  unsigned long long *stats = nullptr, *count[2] = {nullptr, nullptr}, *hst = nullptr;
+  cudaStream_t st = nullptr, cp = nullptr, sl = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr, fork = nullptr, copied[2] = {nullptr, nullptr},
-              consumed[2] = {nullptr, nullptr};
+              consumed[2] = {nullptr, nullptr}, stamped = nullptr, selected = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int dev = 0, sms = 0, per_sm = 0;
@@ -503,9 +508,14 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_select_free_list, FREE_BT, 0);
   const uint64_t grid_sel = (uint64_t)sms * (per_sm > 0 ? per_sm : 1);
-  // one step on st (copies forked onto cp and joined back through the events)
+  auto sel_grid = [&](uint64_t nscan) {
+    const uint64_t chunk = (uint64_t)(FREE_BT / 32) * galwl::WARP_SLOTS;
+    return (unsigned)std::min<uint64_t>((nscan + chunk - 1) / chunk, grid_sel);
+  };
   auto enqueue = [&]() -> int {
-    if (cudaEventRecord(fork, st) != cudaSuccess || cudaStreamWaitEvent(cp, fork, 0) != cudaSuccess)
+    if (cudaMemsetAsync(stats, 0, 4 * sizeof(unsigned long long), st) != cudaSuccess) return GAL_ERR_CUDA;
+    if (cudaEventRecord(fork, st) != cudaSuccess || cudaStreamWaitEvent(cp, fork, 0) != cudaSuccess ||
+        cudaStreamWaitEvent(sl, fork, 0) != cudaSuccess)
       return GAL_ERR_CUDA;
     for (uint32_t r = 0; r < rounds && r < 2; r++) {
       if (cudaMemcpyAsync(d_sizes[r], host_sizes + (uint64_t)r * N, N * sizeof(uint64_t),
@@ -513,17 +523,21 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
           cudaEventRecord(copied[r], cp) != cudaSuccess)
         return GAL_ERR_CUDA;
     }
-    if (cudaMemsetAsync(stats, 0, 4 * sizeof(unsigned long long), st) != cudaSuccess) return GAL_ERR_CUDA;
     for (uint32_t r = 0; r <= rounds; r++) {
       const bool drain = r == rounds;
       if (r > 0) {
-        const uint64_t nscan = drain ? nslots : N * r;
-        const uint64_t chunk = (uint64_t)(FREE_BT / 32) * galwl::WARP_SLOTS;
-        const unsigned g = (unsigned)std::min<uint64_t>((nscan + chunk - 1) / chunk, grid_sel);
-        if (cudaMemsetAsync(count, 0, sizeof(unsigned long long), st) != cudaSuccess) return GAL_ERR_CUDA;
-        k_select_free_list<<<g, FREE_BT, 0, st>>>(ptrs, live, freelist, count, nscan, r, seed,
-                                                  drain ? 1 : 0, stats);
-        int e = gal_free_batched_n(h, freelist, count, nscan, st);
+        const int q = (int)(r & 1u);
+        const uint64_t mid = (uint64_t)(r - 1) * N, hi = drain ? nslots : N * r;
+        if (cudaMemsetAsync(count[q], 0, sizeof(unsigned long long), sl) != cudaSuccess) return GAL_ERR_CUDA;
+        if (mid > 0)  // slots of the older rounds: no wait on the round just stamped
+          k_select_free_list<<<sel_grid(mid), FREE_BT, 0, sl>>>(ptrs, live, freelist[q], count[q], 0, mid, r,
+                                                              seed, drain ? 1 : 0, stats);
+        if (cudaStreamWaitEvent(sl, stamped, 0) != cudaSuccess) return GAL_ERR_CUDA;
+        k_select_free_list<<<sel_grid(hi - mid), FREE_BT, 0, sl>>>(ptrs, live, freelist[q], count[q], mid, hi,
+                                                                 r, seed, drain ? 1 : 0, stats);
+        if (cudaEventRecord(selected, sl) != cudaSuccess || cudaStreamWaitEvent(st, selected, 0) != cudaSuccess)
+          return GAL_ERR_CUDA;
+        int e = gal_free_batched_n(h, freelist[q], count[q], hi, st);
         if (e) return e;
       }
       if (drain) break;
@@ -532,7 +546,7 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
       int e = gal_malloc_batched(h, d_sizes[b], N, ptrs + (uint64_t)r * N, st);
       if (e) return e;
       if (cudaEventRecord(consumed[b], st) != cudaSuccess) return GAL_ERR_CUDA;
-      if (r + 2 < rounds) {  // refill this buffer with round r + 2 while the GPU works
+      if (r + 2 < rounds) {
         if (cudaStreamWaitEvent(cp, consumed[b], 0) != cudaSuccess ||
             cudaMemcpyAsync(d_sizes[b], host_sizes + (uint64_t)(r + 2) * N, N * sizeof(uint64_t),
                             cudaMemcpyHostToDevice, cp) != cudaSuccess ||
@@ -541,6 +555,7 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
       }
       k_stamp_payload<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(ptrs, live, (uint64_t)r * N, N,
                                                                    seed, stats);
+      if (cudaEventRecord(stamped, st) != cudaSuccess) return GAL_ERR_CUDA;
     }
     if (cudaMemcpyAsync(hst, stats, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st) !=
         cudaSuccess)
@@ -549,19 +564,22 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
   };
   CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&cp, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&sl, cudaStreamNonBlocking));
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   CK(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&stamped, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&selected, cudaEventDisableTiming));
   for (int b = 0; b < 2; b++) {
     CK(cudaEventCreateWithFlags(&copied[b], cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&consumed[b], cudaEventDisableTiming));
     CK(cudaMalloc(&d_sizes[b], N * sizeof(uint64_t)));
+    CK(cudaMalloc(&freelist[b], nslots * sizeof(void *)));
+    CK(cudaMalloc(&count[b], sizeof(unsigned long long)));
   }
   CK(cudaMalloc(&ptrs, nslots * sizeof(void *)));
-  CK(cudaMalloc(&freelist, nslots * sizeof(void *)));
   CK(cudaMalloc(&live, nslots / 8));
   CK(cudaMalloc(&stats, 4 * sizeof(unsigned long long)));
-  CK(cudaMalloc(&count, sizeof(unsigned long long)));
   CK(cudaMallocHost(&hst, 4 * sizeof(unsigned long long)));
   CK(cudaMemsetAsync(ptrs, 0, nslots * sizeof(void *), st));
   CK(cudaMemsetAsync(live, 0, nslots / 8, st));
@@ -597,7 +615,7 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
       res->frees += hst[3];
       res->malloc_launches += rounds;
       res->free_launches += rounds;
-      res->other_launches += 2 * rounds;
+      res->other_launches += 3 * rounds;
     }
   }
   res->h2d_bytes = nslots * sizeof(uint64_t);
@@ -606,24 +624,28 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
 done:
   if (st) cudaStreamSynchronize(st);
   if (cp) cudaStreamSynchronize(cp);
+  if (sl) cudaStreamSynchronize(sl);
   if (exec) cudaGraphExecDestroy(exec);
   if (graph) cudaGraphDestroy(graph);
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
   if (fork) cudaEventDestroy(fork);
+  if (stamped) cudaEventDestroy(stamped);
+  if (selected) cudaEventDestroy(selected);
   for (int b = 0; b < 2; b++) {
     if (copied[b]) cudaEventDestroy(copied[b]);
     if (consumed[b]) cudaEventDestroy(consumed[b]);
     if (d_sizes[b]) cudaFree(d_sizes[b]);
+    if (freelist[b]) cudaFree(freelist[b]);
+    if (count[b]) cudaFree(count[b]);
   }
   if (ptrs) cudaFree(ptrs);
   if (live) cudaFree(live);
-  if (freelist) cudaFree(freelist);
   if (stats) cudaFree(stats);
-  if (count) cudaFree(count);
   if (hst) cudaFreeHost(hst);
   if (st) cudaStreamDestroy(st);
   if (cp) cudaStreamDestroy(cp);
+  if (sl) cudaStreamDestroy(sl);
   return rc;
 }
 
