@@ -482,8 +482,9 @@ done:
  * The selection runs on a third stream in two parts: the slots of the older
  * rounds as soon as the previous selection is done (overlapping the previous
  * round's free, malloc and stamp), the slots of the round just stamped after
- * its stamp; the two free lists alternate between rounds.  Each round still
- * frees before it allocates.  use_graph: the step (all three streams, copies
+ * its stamp; each part's frees are served as soon as it is selected (the first
+ * part's while the second is selected), from lists that alternate between
+ * rounds.  Each round still frees before it allocates.  use_graph: the step (all three streams, copies
  * included) is captured once as a CUDA graph, as a user replaying the same
  * step would. */
 int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t threads_per_round,
@@ -493,13 +494,13 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
   if (threads_per_round % galwl::SLOT_ALIGN) return GAL_ERR_ARGS;
   int rc = GAL_OK;
   const uint64_t N = threads_per_round, nslots = N * rounds;
-  void **ptrs = nullptr, **freelist[2] = {nullptr, nullptr};
+  void **ptrs = nullptr, **freelist[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
   uint32_t *live = nullptr;
   uint64_t *d_sizes[2] = {nullptr, nullptr};
-  unsigned long long *stats = nullptr, *count[2] = {nullptr, nullptr}, *hst = nullptr;
+  unsigned long long *stats = nullptr, *count[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}}, *hst = nullptr;
   cudaStream_t st = nullptr, cp = nullptr, sl = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr, fork = nullptr, copied[2] = {nullptr, nullptr},
-              consumed[2] = {nullptr, nullptr}, stamped = nullptr, selected = nullptr;
+              consumed[2] = {nullptr, nullptr}, stamped = nullptr, selected[2] = {nullptr, nullptr};
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int dev = 0, sms = 0, per_sm = 0;
@@ -526,19 +527,26 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
     for (uint32_t r = 0; r <= rounds; r++) {
       const bool drain = r == rounds;
       if (r > 0) {
+        // part 0: the older rounds' slots, selected without waiting for the
+        // round just stamped and freed while part 1 (that round's slots) is
+        // still being selected
         const int q = (int)(r & 1u);
         const uint64_t mid = (uint64_t)(r - 1) * N, hi = drain ? nslots : N * r;
-        if (cudaMemsetAsync(count[q], 0, sizeof(unsigned long long), sl) != cudaSuccess) return GAL_ERR_CUDA;
-        if (mid > 0)  // slots of the older rounds: no wait on the round just stamped
-          k_select_free_list<<<sel_grid(mid), FREE_BT, 0, sl>>>(ptrs, live, freelist[q], count[q], 0, mid, r,
-                                                              seed, drain ? 1 : 0, stats);
-        if (cudaStreamWaitEvent(sl, stamped, 0) != cudaSuccess) return GAL_ERR_CUDA;
-        k_select_free_list<<<sel_grid(hi - mid), FREE_BT, 0, sl>>>(ptrs, live, freelist[q], count[q], mid, hi,
-                                                                 r, seed, drain ? 1 : 0, stats);
-        if (cudaEventRecord(selected, sl) != cudaSuccess || cudaStreamWaitEvent(st, selected, 0) != cudaSuccess)
-          return GAL_ERR_CUDA;
-        int e = gal_free_batched_n(h, freelist[q], count[q], hi, st);
-        if (e) return e;
+        const uint64_t lo_of[2] = {0, mid}, hi_of[2] = {mid, hi};
+        for (int part = 0; part < 2; part++) {
+          if (part == 1 && cudaStreamWaitEvent(sl, stamped, 0) != cudaSuccess) return GAL_ERR_CUDA;
+          if (hi_of[part] == lo_of[part]) continue;
+          if (cudaMemsetAsync(count[q][part], 0, sizeof(unsigned long long), sl) != cudaSuccess)
+            return GAL_ERR_CUDA;
+          k_select_free_list<<<sel_grid(hi_of[part] - lo_of[part]), FREE_BT, 0, sl>>>(
+              ptrs, live, freelist[q][part], count[q][part], lo_of[part], hi_of[part], r, seed,
+              drain ? 1 : 0, stats);
+          if (cudaEventRecord(selected[part], sl) != cudaSuccess ||
+              cudaStreamWaitEvent(st, selected[part], 0) != cudaSuccess)
+            return GAL_ERR_CUDA;
+          int e = gal_free_batched_n(h, freelist[q][part], count[q][part], hi_of[part] - lo_of[part], st);
+          if (e) return e;
+        }
       }
       if (drain) break;
       const int b = (int)(r & 1u);
@@ -569,13 +577,16 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
   CK(cudaEventCreate(&e1));
   CK(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&stamped, cudaEventDisableTiming));
-  CK(cudaEventCreateWithFlags(&selected, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&selected[0], cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&selected[1], cudaEventDisableTiming));
   for (int b = 0; b < 2; b++) {
     CK(cudaEventCreateWithFlags(&copied[b], cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&consumed[b], cudaEventDisableTiming));
     CK(cudaMalloc(&d_sizes[b], N * sizeof(uint64_t)));
-    CK(cudaMalloc(&freelist[b], nslots * sizeof(void *)));
-    CK(cudaMalloc(&count[b], sizeof(unsigned long long)));
+    for (int part = 0; part < 2; part++) {
+      CK(cudaMalloc(&freelist[b][part], nslots * sizeof(void *)));
+      CK(cudaMalloc(&count[b][part], sizeof(unsigned long long)));
+    }
   }
   CK(cudaMalloc(&ptrs, nslots * sizeof(void *)));
   CK(cudaMalloc(&live, nslots / 8));
@@ -615,7 +626,7 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
       res->frees += hst[3];
       res->malloc_launches += rounds;
       res->free_launches += rounds;
-      res->other_launches += 3 * rounds;
+      res->other_launches += 3 * rounds;  // two selection parts and the stamp
     }
   }
   res->h2d_bytes = nslots * sizeof(uint64_t);
@@ -631,13 +642,16 @@ done:
   if (e1) cudaEventDestroy(e1);
   if (fork) cudaEventDestroy(fork);
   if (stamped) cudaEventDestroy(stamped);
-  if (selected) cudaEventDestroy(selected);
+  for (int part = 0; part < 2; part++)
+    if (selected[part]) cudaEventDestroy(selected[part]);
   for (int b = 0; b < 2; b++) {
     if (copied[b]) cudaEventDestroy(copied[b]);
     if (consumed[b]) cudaEventDestroy(consumed[b]);
     if (d_sizes[b]) cudaFree(d_sizes[b]);
-    if (freelist[b]) cudaFree(freelist[b]);
-    if (count[b]) cudaFree(count[b]);
+    for (int part = 0; part < 2; part++) {
+      if (freelist[b][part]) cudaFree(freelist[b][part]);
+      if (count[b][part]) cudaFree(count[b][part]);
+    }
   }
   if (ptrs) cudaFree(ptrs);
   if (live) cudaFree(live);
