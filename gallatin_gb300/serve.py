@@ -59,6 +59,44 @@ def vector_checksum(job_id, n):
     return int((x >> np.uint64(32)).sum(dtype=np.uint64))
 
 
+def schedule(jobs, slots, budget, launch, clock, realtime=True):
+    """The admission loop.  jobs: dicts with kind, n, arrival and row.  A job is
+    admitted in arrival order once it has arrived (realtime) or at once, as
+    soon as a slot is free and the estimated footprints of the running jobs
+    plus its own fit in `budget`; a job that does not fit even alone runs
+    alone.  launch(job, slot) starts it and returns an object whose query()
+    says whether it has finished; clock() gives seconds since the start.
+    Returns the admission and completion times per row and the most jobs that
+    ran at once."""
+    nj = len(jobs)
+    pending = deque(sorted(jobs, key=lambda j: j["arrival"]))
+    free_slots = list(range(slots))
+    running = {}
+    reserved = 0
+    admit_t, done_t = np.zeros(nj), np.zeros(nj)
+    max_running = 0
+    while pending or running:
+        now = clock()
+        for slot, (job, ev) in list(running.items()):
+            if ev.query():
+                done_t[job["row"]] = clock()
+                reserved -= job["est"]
+                free_slots.append(slot)
+                del running[slot]
+        while pending and free_slots and (not realtime or pending[0]["arrival"] <= now):
+            job = pending[0]
+            job["est"] = footprint(job["kind"], job["n"])
+            if running and reserved + job["est"] > budget:
+                break                          # wait for memory to free up
+            pending.popleft()
+            slot = free_slots.pop()
+            running[slot] = (job, launch(job, slot))
+            reserved += job["est"]
+            admit_t[job["row"]] = clock()
+            max_running = max(max_running, len(running))
+    return admit_t, done_t, max_running
+
+
 class Server:
     def __init__(self, g: Gallatin, slots=32, budget_bytes=None):
         import torch
@@ -82,38 +120,17 @@ class Server:
         lats = torch.zeros((nj, 2 * LAT), dtype=torch.int32, device="cuda")
         torch.cuda.synchronize()
         jobs = [dict(j, row=r) for r, j in enumerate(jobs)]  # result rows follow the input order
-        pending = deque(sorted(jobs, key=lambda j: j["arrival"]))
-        free_slots = list(range(self.slots))
-        running = {}
-        reserved = 0
-        admit_t, done_t = np.zeros(nj), np.zeros(nj)
-        max_running = 0
+
+        def launch(job, slot):
+            s = self.streams[slot]
+            self._launch(job, job["row"], results, lats, s)
+            ev = torch.cuda.Event()
+            ev.record(s)
+            return ev
+
         t0 = time.perf_counter()
-        while pending or running:
-            now = time.perf_counter() - t0
-            for slot, (job, ev) in list(running.items()):
-                if ev.query():
-                    done_t[job["row"]] = time.perf_counter() - t0
-                    reserved -= job["est"]
-                    free_slots.append(slot)
-                    del running[slot]
-            while pending and free_slots and (not realtime or pending[0]["arrival"] <= now):
-                job = pending[0]
-                job["est"] = footprint(job["kind"], job["n"])
-                if running and reserved + job["est"] > self.budget:
-                    break                          # wait for memory to free up
-                pending.popleft()
-                slot = free_slots.pop()
-                s = self.streams[slot]
-                self._launch(job, job["row"], results, lats, s)
-                ev = torch.cuda.Event()
-                ev.record(s)
-                running[slot] = (job, ev)
-                reserved += job["est"]
-                admit_t[job["row"]] = time.perf_counter() - t0
-                max_running = max(max_running, len(running))
-            if not realtime and not pending and not running:
-                break
+        admit_t, done_t, max_running = schedule(jobs, self.slots, self.budget, launch,
+                                                lambda: time.perf_counter() - t0, realtime)
         wall = time.perf_counter() - t0
         torch.cuda.synchronize()
         res = results.cpu().numpy()
