@@ -209,3 +209,31 @@ def test_warp_traces_on_other_geometries_match_oracle(G, geom):
         assert g.error_word() == 0
     finally:
         g.close()
+
+
+@pytest.mark.parametrize("kind", ["serial", "warp"])
+def test_one_slot_per_sm_geometry_matches_oracle(G, kind):
+    """The throughput geometry (64 MiB segments, one pinned slot per SM in
+    every class, lock-free gathers) without spare blocks: serial and warp-team
+    traces equal the oracle with as many slots as the GPU has SMs."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    cfg = dict(bytes_per_segment=64 << 20, pinned_slots_first=0, pinned_slots_min=0,
+               gather_unlocked_below=16)
+    g = G.Gallatin.generate_on_device(16 << 30, 5, **cfg)
+    try:
+        o = Oracle(16 << 30, 5, bytes_per_segment=64 << 20, pinned_first=sms, pinned_min=sms,
+                   fixes=PRODUCT_FIXES)
+        assert g.export().diff(o.export()) == []       # the same boot
+        if kind == "serial":
+            ops = gen_log_trace(808, 20000, 55, 4, 20)
+            out, smid = g.replay(ops)
+            np.testing.assert_array_equal(out, o.replay(ops, smid=smid))
+        else:
+            steps = gen_warp_trace(818, 2500, tree_weights=(4, 2, 1, 1, 1, 1, 1, 2, 3), big_pct=40)
+            out, smid = g.replay_warp(steps)
+            np.testing.assert_array_equal(out, o.replay_warp(steps, smid=smid))
+        assert g.export().diff(o.export()) == []
+        assert g.error_word() == 0
+    finally:
+        g.close()
