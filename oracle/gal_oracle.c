@@ -374,6 +374,8 @@ struct orc_alloc {
   int32_t *queues;
   int nslots[MAXT];
   int32_t *slots[MAXT];
+  int32_t *spares[MAXT]; /* the product's spare blocks (orc_set_spares) */
+  int use_spares;
   uint32_t locks;
 };
 
@@ -430,7 +432,8 @@ orc_alloc *orc_create(uint64_t num_bytes, uint64_t seed, uint64_t seg_bytes, uin
     uint64_t cnt = n == 0 ? 1 : n;
     a->nslots[t] = (int)cnt;
     a->slots[t] = (int32_t *)malloc(cnt * sizeof(int32_t));
-    for (uint64_t i = 0; i < cnt; i++) a->slots[t][i] = NOBLK;
+    a->spares[t] = (int32_t *)malloc(cnt * sizeof(int32_t));
+    for (uint64_t i = 0; i < cnt; i++) a->slots[t][i] = a->spares[t][i] = NOBLK;
     n = n / 2;
     if (n < pinned_min) n = pinned_min;
   }
@@ -444,6 +447,7 @@ void orc_destroy(orc_alloc *a) {
   for (int i = 0; i < a->num_trees; i++) {
     free(a->sub[i].w);
     free(a->slots[i]);
+    free(a->spares[i]);
   }
   free(a->tree_ids);
   free(a->active);
@@ -615,11 +619,13 @@ static void free_offset(orc_alloc *a, uint64_t offset) {
  * handed out so that a block with nothing live goes back to its segment, then
  * boot the slots again in the one-thread order. */
 int orc_trim(orc_alloc *a) {
+  for (int pass = 0; pass < 2; pass++) /* spare blocks first, then the slots */
   for (int tree = 0; tree < a->num_trees; tree++)
     for (int i = 0; i < a->nslots[tree]; i++) {
-      int32_t blk = a->slots[tree][i];
+      int32_t *cell = pass == 0 ? &a->spares[tree][i] : &a->slots[tree][i];
+      int32_t blk = *cell;
       if (blk == NOBLK) continue;
-      a->slots[tree][i] = NOBLK;
+      *cell = NOBLK;
       uint32_t merged = a->mc[blk];
       a->mc[blk] = merged + 4096u;
       uint32_t c = merged & 0xFFFFFu;
@@ -671,6 +677,35 @@ static int replace_block(orc_alloc *a, int tree, int slot, int32_t blk, uint64_t
   return 1;
 }
 
+/* The product's spare blocks (gal_config.spare_blocks; no reference
+ * counterpart): the crossing lane's team leader swaps the slot's prepared
+ * block in instead of searching for one, falling back to replace_block when
+ * none is ready, and then prepares the next one with its own thread id.  A
+ * single thread always finds the slot still holding the exhausted block. */
+static void replace_or_swap(orc_alloc *a, int tree, int slot, int32_t blk, uint64_t tid) {
+  if (!a->use_spares) {
+    replace_block(a, tree, slot, blk, tid);
+    return;
+  }
+  int32_t nx = a->spares[tree][slot];
+  a->spares[tree][slot] = NOBLK;
+  if (nx == NOBLK) {
+    replace_block(a, tree, slot, blk, tid);
+  } else if (a->slots[tree][slot] != blk) {
+    a->fc[nx] = 0; /* the slot moved on: all 4096 slices credited, the spare goes back */
+    free_block(a, nx);
+    return;
+  } else {
+    a->slots[tree][slot] = nx;
+  }
+  if (a->spares[tree][slot] == NOBLK) {
+    int32_t nb = request_new_block(a, tree, tid);
+    if (nb != NOBLK) a->spares[tree][slot] = nb;
+  }
+}
+
+void orc_set_spares(orc_alloc *a, int on) { a->use_spares = on != 0; }
+
 /* Gallatin::malloc_slice_allocation (gallatin.cuh:865-1078), team of one.
  * The reference's 500 attempts are kept: a failed attempt can replace the
  * pinned block, so a retry can succeed. */
@@ -697,7 +732,7 @@ static uint64_t malloc_slice(orc_alloc *a, int tree, uint32_t alloc_count, uint3
       }
     }
     if (allocation + alloc_count > 4096) allocation = ORC_FAIL;
-    if (should_replace) replace_block(a, tree, slot, blk, tid);
+    if (should_replace) replace_or_swap(a, tree, slot, blk, tid);
     if (allocation != ORC_FAIL) {
       if ((merged >> 20) != (uint32_t)tree) { /* Block::check_valid */
         free_offset(a, allocation + gbid * 4096);
@@ -753,7 +788,7 @@ static void malloc_slice_team(orc_alloc *a, int tree, const uint32_t *counts, ui
         free_block(a, blk);
       }
     }
-    if (should_replace) replace_block(a, tree, slot, blk, tid0 + (uint64_t)leader);
+    if (should_replace) replace_or_swap(a, tree, slot, blk, tid0 + (uint64_t)leader);
     for (int l = 0; l < 32; l++) {
       if (!((pending >> l) & 1u) || alloc[l] == ORC_FAIL) continue;
       uint64_t off = alloc[l] + (uint64_t)blk * 4096;
@@ -975,6 +1010,7 @@ int orc_import(orc_alloc *a, const gal_state_view *v) {
   uint64_t o = 0;
   for (int t = 0; t < a->num_trees; t++) {
     memcpy(a->slots[t], v->slots + o, (uint64_t)a->nslots[t] * 4);
+    for (int i = 0; i < a->nslots[t]; i++) a->spares[t][i] = NOBLK; /* the view holds none */
     o += (uint64_t)a->nslots[t];
   }
   a->locks = v->locks;

@@ -36,6 +36,9 @@ orc_alloc *orc_create(uint64_t num_bytes, uint64_t seed, uint64_t bytes_per_segm
                       uint32_t pinned_min, uint32_t fix_flags, uint32_t policy);
 void orc_destroy(orc_alloc *a);
 
+/* model the product's spare blocks (gal_config.spare_blocks = 1) */
+void orc_set_spares(orc_alloc *a, int on);
+
 /* boot_shared_block_container_one_thread (gallatin.cuh:196-221), thread id 0 */
 int orc_boot_one_thread(orc_alloc *a);
 

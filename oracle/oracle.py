@@ -41,6 +41,7 @@ def lib():
         L.orc_destroy.argtypes = [C.c_void_p]
         L.orc_boot_one_thread.argtypes = [C.c_void_p]
         L.orc_trim.argtypes = [C.c_void_p]
+        L.orc_set_spares.argtypes = [C.c_void_p, C.c_int]
         L.orc_malloc.restype = C.c_uint64
         L.orc_malloc.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint64]
         L.orc_free.argtypes = [C.c_void_p, C.c_uint64]
@@ -161,11 +162,12 @@ class Oracle:
 
     def __init__(self, num_bytes, seed, bytes_per_segment=16 << 20, min_size=16, max_size=4096,
                  pinned_first=128, pinned_min=4, fixes=PRODUCT_FIXES, policy=GAL_POLICY_REFERENCE,
-                 boot=True):
+                 boot=True, spares=False):
         self._h = lib().orc_create(num_bytes, seed, bytes_per_segment, min_size, max_size,
                                    pinned_first, pinned_min, fixes, policy)
         if not self._h:
             raise RuntimeError("orc_create failed")
+        lib().orc_set_spares(self._h, 1 if spares else 0)
         self.bytes_per_segment = bytes_per_segment
         if boot:
             r = lib().orc_boot_one_thread(self._h)

@@ -237,3 +237,29 @@ def test_one_slot_per_sm_geometry_matches_oracle(G, kind):
         assert g.error_word() == 0
     finally:
         g.close()
+
+
+@pytest.mark.parametrize("kind", ["serial", "warp"])
+def test_spare_blocks_match_oracle(G, kind):
+    """spare_blocks = 1 on the per-thread path: the block that crosses slice
+    4095 is replaced by the slot's prepared spare and the next spare is
+    requested at once; the oracle's model of it gives the same offsets and
+    state, and so does a trim afterwards (spares retired first)."""
+    g = G.Gallatin.generate_on_device(2 << 30, 42, spare_blocks=1)
+    try:
+        o = Oracle(2 << 30, 42, fixes=PRODUCT_FIXES, spares=True)
+        if kind == "serial":
+            ops = gen_serial_trace(909, 30000, 58, 16, 256)
+            out, smid = g.replay(ops)
+            np.testing.assert_array_equal(out, o.replay(ops, smid=smid))
+        else:
+            steps = gen_warp_trace(919, 3000, tree_weights=(6, 3, 1, 1, 1, 1, 1, 2, 3), big_pct=40)
+            out, smid = g.replay_warp(steps)
+            np.testing.assert_array_equal(out, o.replay_warp(steps, smid=smid))
+        assert g.export().diff(o.export()) == []
+        g.trim()
+        o.trim()
+        assert g.export().diff(o.export()) == []
+        assert g.error_word() == 0
+    finally:
+        g.close()
