@@ -503,10 +503,22 @@ GAL_DEVICE_COLD int64_t gather_new_segment(const state *s, uint32_t tree) {
 // alloc_table::get_block (memory_table.cuh:915-993)
 GAL_DEVICE_COLD uint32_t get_block(const state *s, uint64_t seg, uint32_t tree, bool &last) {
   last = false;
-  int ac = atomicSub(&s->active[seg], 1);
-  if (ac < 0) {
-    atomicAdd(&s->active[seg], 1);
-    return NOBLK;
+  // Reserve one of the segment's blocks without ever taking the count below
+  // zero.  The reference subtracts and adds back on failure
+  // (memory_table.cuh:923-929, get_slot_in_segment / return_slot_to_segment);
+  // an add-back that lands after the segment was released and set up again
+  // raises the new count above the blocks the segment has, and later
+  // hand-outs then meet empty ring entries and releases come early.
+  int ac = ld_rlx(&s->active[seg]);
+  for (uint32_t i = 0;; i++) {
+    if (ac < 0) return NOBLK;
+    const int seen = atomicCAS(&s->active[seg], ac, ac - 1);
+    if (seen == ac) break;
+    ac = seen;
+    if (i >= s->spin_limit) {
+      set_error(s, GAL_DEV_ERR_TIMEOUT);
+      return NOBLK;
+    }
   }
   __threadfence();
   if (ld_rlx(&s->tree_ids[seg]) != (uint16_t)tree) {
@@ -732,16 +744,20 @@ GAL_DEVICE_INLINE char *slice_ptr(const state *s, uint32_t blk, uint64_t idx, ui
 
 // ------------------------------------------------------------------ malloc tiers
 // Gallatin::malloc_slice_allocation (gallatin.cuh:865-1078): warp team per
-// size class, one atomicAdd on the pinned block per team.  `pending` holds the
-// lanes that called malloc together and ask for slices (the coalesced group
-// the reference partitions); it shrinks as lanes get their slices, and every
-// warp-wide step of an attempt names it, so a team always holds every caller
-// of its class even when the caller's branches ran as separate groups.
+// size class, one atomicAdd on the pinned block per team.  Two ways to know
+// the team: as the reference does, the lanes executing each attempt together
+// (NAMED = false: every attempt re-forms the teams from the active lanes, and
+// a lane leaves the loop as soon as it has its slice); or named by the caller
+// (NAMED = true: `pending`, the lanes that called together and ask for
+// slices, shrinks as lanes get their slices, and every warp-wide step of an
+// attempt names it, so a team holds every caller of its class even when the
+// callers' earlier branches left them in separate groups).
+template <bool NAMED>
 GAL_DEVICE_INLINE void *malloc_slices(const state *s, uint32_t tree, uint32_t count, uint32_t pending) {
   const uint32_t lane = lane_id();
   const uint64_t tid = thread_linear_id();
   for (int attempt = 0; attempt < SLICE_ATTEMPTS; attempt++) {
-    const uint32_t active = pending;
+    const uint32_t active = NAMED ? pending : active_lanes();
     const uint32_t team = __match_any_sync(active, tree) & team_group(s);
     const int leader = __ffs(team) - 1;
     const int last = 31 - __clz(team);
@@ -753,6 +769,7 @@ GAL_DEVICE_INLINE void *malloc_slices(const state *s, uint32_t tree, uint32_t co
     const uint32_t blk = __shfl_sync(active, seen, leader);
     // teams whose slot was empty retry; the rest carry on with mask `live`
     const uint32_t live = __ballot_sync(active, blk != NOBLK);
+    if (!NAMED && blk == NOBLK) continue;
     void *result = nullptr;
     bool refill = false;
     if (blk != NOBLK) {
@@ -784,13 +801,16 @@ GAL_DEVICE_INLINE void *malloc_slices(const state *s, uint32_t tree, uint32_t co
         else replace_block(s, tree, slot, blk, tid);
       }
       __syncwarp(live);
+      if (!NAMED && refill) refill_spare(s, tree, slot, tid);  // the team's other lanes go on
       if (start_valid && end_valid) {
         if ((uint32_t)(old >> 32) == tree) result = slice_ptr(s, blk, alloc, tree);
         else credit_frees(s, blk, 1);  // Block::check_valid failed: give the slice back
       }
     }
-    pending = __ballot_sync(active, result == nullptr);
-    if (refill) refill_spare(s, tree, slot, tid);  // the team's other lanes go on
+    if (NAMED) {
+      pending = __ballot_sync(active, result == nullptr);
+      if (refill) refill_spare(s, tree, slot, tid);  // the team's other lanes go on
+    }
     if (result) return result;
   }
   return nullptr;
@@ -859,32 +879,37 @@ GAL_DEVICE_COLD void *malloc_large(const state *s, uint64_t size, int block_tree
 }
 
 // Gallatin::malloc (gallatin.cuh:1186-1276) called by the lanes in `callers`
-// together: every lane of the mask calls with the same mask (the contract of
-// the *_sync warp intrinsics).  Those that ask for slices form the claim teams,
-// one per size class, and reach malloc_slices on one path (the class and run
-// length are selects, not branches).
-GAL_DEVICE_INLINE void *malloc_team(const state *s, uint64_t size, uint32_t callers) {
-  const uint32_t entered = callers;
+// together.  Those that ask for slices reach malloc_slices on one path (the
+// class and run length are selects, not branches), so single slices and runs
+// of the same class share a team.
+template <bool NAMED>
+GAL_DEVICE_INLINE void *malloc_from(const state *s, uint64_t size, uint32_t callers) {
   const int T = (int)s->num_trees;
   const int bits = ceil_log2(size);
   const int t = (size >> s->min_shift) == 0 ? 0 : bits - (int)s->min_shift;
   const int block_tree = bits - (int)(s->min_shift + 12);
   const bool slices = t < T || block_tree < 0;
-  const uint32_t members = __ballot_sync(entered, slices);
+  const uint32_t members = __ballot_sync(callers, slices);
   if (!slices) return handed_out(s, malloc_large(s, size, block_tree), size);
   // big slices (4 KiB < size <= 32 KiB by default): runs of the last class
   const bool big = t >= T;
   const uint32_t count = 1u << (big ? t - (T - 1) : 0);
   const uint32_t tree = (uint32_t)(big ? T - 1 : t);
-  return handed_out(s, malloc_slices(s, tree, count, members), size);
+  return handed_out(s, malloc_slices<NAMED>(s, tree, count, members), size);
 }
 
-// Gallatin::malloc as the reference calls it: the team is the lanes executing
-// the call together (its coalesced_threads(), gallatin.cuh:883).  Which lanes
-// those are after divergence is the scheduler's choice, in either build; a
-// caller that knows its callers names them with malloc_team.
+// Gallatin::malloc as the reference calls it: each attempt's team is the lanes
+// executing it together (its coalesced_threads(), gallatin.cuh:883).
 GAL_DEVICE_INLINE void *malloc(const state *s, uint64_t size) {
-  return malloc_team(s, size, active_lanes());
+  return malloc_from<false>(s, size, active_lanes());
+}
+
+// malloc with the calling lanes named: every lane of `callers` calls with the
+// same mask (the contract of the *_sync warp intrinsics), and the lanes asking
+// for slices of one class form one team whatever grouping of diverged lanes
+// the scheduler chose.
+GAL_DEVICE_INLINE void *malloc_team(const state *s, uint64_t size, uint32_t callers) {
+  return malloc_from<true>(s, size, callers);
 }
 
 // multi-segment free (gallatin.cuh:1394-1417, 1283-1302), id reset first
