@@ -49,6 +49,34 @@ def test_default_config_is_reference_geometry(L):
     assert (cfg.pinned_slots_first, cfg.pinned_slots_min) == (128, 4)
     assert cfg.smid_override == -1 and cfg.subtree_policy == G.GAL_POLICY_REFERENCE
     assert cfg.team_width == 32
+    assert (cfg.arena_kind, cfg.spare_blocks, cfg.zero_fill) == (G._abi.GAL_ARENA_DEVICE, 0, 0)
+
+
+@pytest.mark.parametrize("ctype,mirror", [("gal_config", "GalConfig"), ("gal_stats", "GalStats"),
+                                           ("gal_state_dims", "GalStateDims"),
+                                           ("gal_state_view", "GalStateViewC")])
+def test_ctypes_mirrors_have_the_header_layout(tmp_path, ctype, mirror):
+    """Each ctypes mirror of a struct in include/gallatin_gb300.h has the C
+    struct's size and field offsets (a C program compiled against the header
+    prints them)."""
+    import shutil
+    import subprocess
+
+    import gallatin_gb300 as G
+    if not shutil.which("gcc"):
+        pytest.skip("gcc absent")
+    cls = getattr(G._abi, mirror)
+    fields = [f[0] for f in cls._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text("#include <stdio.h>\n#include <stddef.h>\n#include \"gallatin_gb300.h\"\n"
+                   "int main(void) {\n" + f'  printf("%zu\\n", sizeof({ctype}));\n' +
+                   "".join(f'  printf("%zu\\n", offsetof({ctype}, {f}));\n' for f in fields) +
+                   "  return 0;\n}\n")
+    exe = tmp_path / "layout"
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    got = [int(x) for x in subprocess.check_output([str(exe)]).split()]
+    assert got[0] == C.sizeof(cls)
+    assert got[1:] == [getattr(cls, f).offset for f in fields]
 
 
 @pytest.mark.parametrize("kw", [
