@@ -66,8 +66,11 @@ def free_everything(ops):
     (lambda: gen_serial_trace(101, 20000, 55, 16, 256), 2 << 30),
     (lambda: gen_log_trace(404, 4000, 55, 4, 26), 16 << 30),
 ])
-def test_trim_after_freeing_everything_restores_fresh_trees(mk, nbytes):
-    o = Oracle(nbytes, 42)
+@pytest.mark.parametrize("spares", [False, True], ids=["", "spares"])
+def test_trim_after_freeing_everything_restores_fresh_trees(mk, nbytes, spares):
+    """With spare blocks (the product's gal_config.spare_blocks) trim retires
+    the spares first, so the same fresh state comes back."""
+    o = Oracle(nbytes, 42, spares=spares)
     fresh = o.export()
     o.replay(free_everything(mk()))
     assert o.export().diff(fresh, fields=TREE_FIELDS) != []  # pinned blocks still partly used
