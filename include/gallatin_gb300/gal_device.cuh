@@ -389,8 +389,8 @@ GAL_DEVICE_COLD uint64_t veb_gather_run(const veb_ref &v, uint64_t needed) {
     n -= (uint64_t)c;
     bool ok = true;
     while (n > 64) {
-      if (sb == 0) {  // run would leave the arena (the reference indexes word -1)
-        veb_rollback(v, 1, needed - n);
+      if (sb == 0) {  // run would leave the arena (the reference indexes word -1):
+        veb_rollback(v, sb, needed - n);  // give back words 0 .. the first one
         return FAIL;
       }
       sb--;
@@ -404,8 +404,8 @@ GAL_DEVICE_COLD uint64_t veb_gather_run(const veb_ref &v, uint64_t needed) {
       n -= 64;
     }
     if (!ok) continue;
-    if (sb == 0) {
-      veb_rollback(v, 1, needed - n);
+    if (sb == 0) {  // the same: the words taken start at word 0
+      veb_rollback(v, sb, needed - n);
       return FAIL;
     }
     sb--;

@@ -266,6 +266,10 @@ static uint64_t layer_gather_multiple(veb *v, uint64_t num_contiguous, uint32_t 
     if (popc64(got & bitmask(contig_start)) == contig_start) {
       num_contiguous -= (uint64_t)contig_start;
       while (num_contiguous > 64) {
+        if (start_block == 0 && (fix & ORC_FIX_RUN_BELOW_ARENA)) {
+          layer_rollback(v, layer, 0, num_needed - num_contiguous);
+          return ORC_FAIL;
+        }
         start_block--;
         w = vw(v, layer, start_block);
         got = *w;
@@ -279,6 +283,10 @@ static uint64_t layer_gather_multiple(veb *v, uint64_t num_contiguous, uint32_t 
         num_contiguous -= 64;
       }
       if (!succeeded) continue;
+      if (start_block == 0 && (fix & ORC_FIX_RUN_BELOW_ARENA)) {
+        layer_rollback(v, layer, 0, num_needed - num_contiguous);
+        return ORC_FAIL;
+      }
       start_block--;
       w = vw(v, layer, start_block);
       uint64_t fmask = bitmask((int)num_contiguous) << (64 - num_contiguous);

@@ -28,6 +28,10 @@ extern "C" {
  * owed, the block is never returned (leaked).  With the fix the leftover
  * credit completes the block like any other free. */
 #define ORC_FIX_LEFTOVER_COMPLETES 0x2u
+/* veb.cuh:382-410: a run that still needs more than the words below it
+ * steps to word -1.  With the fix the request fails and the words it took
+ * (word 0 up to its first word) are given back. */
+#define ORC_FIX_RUN_BELOW_ARENA 0x4u
 
 typedef struct orc_alloc orc_alloc;
 

@@ -263,3 +263,28 @@ def test_spare_blocks_match_oracle(G, kind):
         assert g.error_word() == 0
     finally:
         g.close()
+
+
+def test_run_below_the_arena_fails_and_gives_back_what_it_took(G):
+    """A multi-segment request that would need segments below segment 0 (the
+    reference indexes bottom-layer word -1, veb.cuh:382-410): it fails, the
+    words it took are given back, and the whole state equals the oracle's."""
+    from tests.test_oracle_runs import RUN_BELOW_ARENA, SEG
+    ops, idx = [], []
+    for op, x in RUN_BELOW_ARENA + [("m", 84), ("m", 64)]:
+        if op == "m":
+            idx.append(len(ops))
+            ops.append(x * SEG)
+        else:
+            ops.append((1 << 63) | idx[x])
+    ops = np.array(ops, dtype=np.uint64)
+    g = G.Gallatin.generate_on_device(2 << 30, 42, boot=False)
+    try:
+        out, smid = g.replay(ops)
+        o = Oracle(2 << 30, 42, fixes=PRODUCT_FIXES, boot=False)
+        np.testing.assert_array_equal(out, o.replay(ops, smid=smid))
+        assert int(out[idx[-2]]) == FAIL and int(out[idx[-1]]) == SEG
+        assert g.export().diff(o.export()) == []
+        assert g.error_word() == 0
+    finally:
+        g.close()
