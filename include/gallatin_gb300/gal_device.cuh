@@ -447,13 +447,18 @@ GAL_DEVICE_COLD void veb_return_multiple(const veb_ref &v, uint64_t start, uint6
     left -= (uint64_t)add;
   }
   amo_or(v.word(bottom, bi), bitmask((int)left) << bs);
+  // maybe_return_layer_bits (veb.cuh:1128-1154) lists a word only when it is
+  // full; an edge word that the claim emptied comes back partly filled and
+  // would stay unlisted (its segments unreachable by every single-item
+  // search).  Every non-empty word is listed here; a listed word that a
+  // racing remove empties again is skipped by veb_successor.
   uint64_t lo = start;
   for (int i = bottom - 1; i >= 0; i--) {
     uint64_t hi = (lo + n - 1) / 64 + 1;
     lo = lo / 64;
     n = hi - lo;
     for (uint64_t wb = lo; wb < lo + n; wb++)
-      if (__popcll(ld_rlx(v.word(i + 1, wb))) == 64) amo_or(v.word(i, wb / 64), 1ULL << (wb % 64));
+      if (ld_rlx(v.word(i + 1, wb)) != 0) amo_or(v.word(i, wb / 64), 1ULL << (wb % 64));
   }
 }
 

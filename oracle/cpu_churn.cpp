@@ -23,7 +23,8 @@ extern "C" {
 double orc_churn_oracle(uint64_t arena_bytes, uint64_t threads_per_round, uint32_t rounds,
                         uint32_t seed, uint64_t *ops_out) {
   orc_alloc *a = orc_create(arena_bytes, 42, 16ull << 20, 16, 4096, 128, 4,
-                            ORC_FIX_GATHER_EXIT_ROLLBACK | ORC_FIX_LEFTOVER_COMPLETES | ORC_FIX_RUN_BELOW_ARENA, 0);
+                            ORC_FIX_GATHER_EXIT_ROLLBACK | ORC_FIX_LEFTOVER_COMPLETES | ORC_FIX_RUN_BELOW_ARENA |
+                                ORC_FIX_RUN_RETURN_SUMMARY, 0);
   orc_boot_one_thread(a);
   const uint64_t nslots = threads_per_round * rounds;
   std::vector<uint64_t> live(nslots, ~0ull);

@@ -350,8 +350,9 @@ static uint64_t veb_gather_multiple(veb *v, uint64_t num_contiguous, uint32_t fi
 }
 
 /* veb_tree::return_multiple (veb.cuh:1198-1218) with
- * maybe_return_layer_bits (veb.cuh:1128-1154) */
-static void veb_return_multiple(veb *v, uint64_t start_bit, uint64_t num_contiguous) {
+ * maybe_return_layer_bits (veb.cuh:1128-1154); ORC_FIX_RUN_RETURN_SUMMARY
+ * lists every word the run made non-empty, not only the full ones */
+static void veb_return_multiple(veb *v, uint64_t start_bit, uint64_t num_contiguous, uint32_t fix) {
   layer_return_multiple(v, v->L - 1, start_bit, num_contiguous);
   for (int i = v->L - 2; i >= 0; i--) {
     uint64_t tread_high = (start_bit + num_contiguous - 1) / 64 + 1;
@@ -359,7 +360,9 @@ static void veb_return_multiple(veb *v, uint64_t start_bit, uint64_t num_contigu
     start_bit = tread_low;
     num_contiguous = tread_high - tread_low;
     for (uint64_t wb = start_bit; wb < start_bit + num_contiguous; wb++) {
-      if (popc64(*vw(v, i + 1, wb)) == 64) layer_insert_bit(v, i, wb / 64, (int)(wb % 64));
+      const uint64_t child = *vw(v, i + 1, wb);
+      const int listed = (fix & ORC_FIX_RUN_RETURN_SUMMARY) ? child != 0 : popc64(child) == 64;
+      if (listed) layer_insert_bit(v, i, wb / 64, (int)(wb % 64));
     }
   }
 }
@@ -886,7 +889,7 @@ void orc_free(orc_alloc *a, uint64_t byte_offset) {
   if (tree == 0xFFFF || tree == (uint16_t)a->num_trees) orc_die("free into a free segment");
   if (tree > a->num_trees) {
     uint16_t count = (uint16_t)(tree - a->num_trees - 1);
-    veb_return_multiple(&a->seg_tree, seg, count);
+    veb_return_multiple(&a->seg_tree, seg, count, a->fix);
     a->tree_ids[seg] = 0xFFFF;
     return;
   }

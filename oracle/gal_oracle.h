@@ -32,6 +32,13 @@ extern "C" {
  * steps to word -1.  With the fix the request fails and the words it took
  * (word 0 up to its first word) are given back. */
 #define ORC_FIX_RUN_BELOW_ARENA 0x4u
+/* veb.cuh:1128-1154: returning a run lists a bottom word in the summary only
+ * when the word is then full.  A run whose claim emptied its first or last
+ * word gives that word back partly filled and unlisted, so the single-item
+ * searches never reach its segments again (nor does a later insert into the
+ * word, which climbs only from an empty word).  With the fix every word the
+ * run leaves non-empty is listed. */
+#define ORC_FIX_RUN_RETURN_SUMMARY 0x8u
 
 typedef struct orc_alloc orc_alloc;
 

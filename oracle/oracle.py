@@ -17,8 +17,10 @@ LIB_PATH = os.path.join(HERE, "liboracle.so")
 FIX_GATHER_EXIT_ROLLBACK = 0x1
 FIX_LEFTOVER_COMPLETES = 0x2
 FIX_RUN_BELOW_ARENA = 0x4
+FIX_RUN_RETURN_SUMMARY = 0x8
 # the product fixes these reference defects; parity runs against the product use them
-PRODUCT_FIXES = FIX_GATHER_EXIT_ROLLBACK | FIX_LEFTOVER_COMPLETES | FIX_RUN_BELOW_ARENA
+PRODUCT_FIXES = (FIX_GATHER_EXIT_ROLLBACK | FIX_LEFTOVER_COMPLETES | FIX_RUN_BELOW_ARENA
+                 | FIX_RUN_RETURN_SUMMARY)
 
 _lib = None
 

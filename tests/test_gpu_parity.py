@@ -269,21 +269,33 @@ def test_run_below_the_arena_fails_and_gives_back_what_it_took(G):
     """A multi-segment request that would need segments below segment 0 (the
     reference indexes bottom-layer word -1, veb.cuh:382-410): it fails, the
     words it took are given back, and the whole state equals the oracle's."""
-    from tests.test_oracle_runs import RUN_BELOW_ARENA, SEG
-    ops, idx = [], []
-    for op, x in RUN_BELOW_ARENA + [("m", 84), ("m", 64)]:
-        if op == "m":
-            idx.append(len(ops))
-            ops.append(x * SEG)
-        else:
-            ops.append((1 << 63) | idx[x])
-    ops = np.array(ops, dtype=np.uint64)
+    from tests.test_oracle_runs import RUN_BELOW_ARENA, SEG, runs_to_ops
+    ops, idx = runs_to_ops(RUN_BELOW_ARENA + [("m", 84), ("m", 64)])
     g = G.Gallatin.generate_on_device(2 << 30, 42, boot=False)
     try:
         out, smid = g.replay(ops)
         o = Oracle(2 << 30, 42, fixes=PRODUCT_FIXES, boot=False)
         np.testing.assert_array_equal(out, o.replay(ops, smid=smid))
         assert int(out[idx[-2]]) == FAIL and int(out[idx[-1]]) == SEG
+        assert g.export().diff(o.export()) == []
+        assert g.error_word() == 0
+    finally:
+        g.close()
+
+
+def test_a_returned_run_lists_every_word_it_refills(G):
+    """Freeing a run lists every bottom word it leaves non-empty, not only the
+    full ones (veb.cuh:1128-1154): after the run pair that empties word 1, the
+    single-segment requests reach all 94 free segments, as in the oracle."""
+    from tests.test_oracle_runs import HIDDEN_BY_RETURN, SEG, runs_to_ops
+    ops, _ = runs_to_ops(HIDDEN_BY_RETURN + [("m", 1)] * 100)
+    g = G.Gallatin.generate_on_device(2 << 30, 42, boot=False)
+    try:
+        out, smid = g.replay(ops)
+        o = Oracle(2 << 30, 42, fixes=PRODUCT_FIXES, boot=False)
+        np.testing.assert_array_equal(out, o.replay(ops, smid=smid))
+        singles = out[3:]
+        assert int((singles != FAIL).sum()) == 94
         assert g.export().diff(o.export()) == []
         assert g.error_word() == 0
     finally:

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from gallatin_gb300._abi import FAIL
-from oracle.oracle import PRODUCT_FIXES, Oracle
+from oracle.oracle import FIX_RUN_RETURN_SUMMARY, PRODUCT_FIXES, Oracle
 
 SEG = 16 << 20
 
@@ -73,3 +73,44 @@ def test_a_run_below_the_arena_fails_and_gives_back_what_it_took():
     assert o.export().diff(before) == []
     # word 0 is whole again: a run of 64 takes segment 64 and the top 63 of it
     assert o.malloc(64 * SEG) == 1 * SEG
+
+
+# Returning a run lists a bottom word in the summary only when the word is then
+# full (maybe_return_layer_bits, veb.cuh:1128-1154).  On 128 segments a run of
+# 34 takes 94-127 and a run of 36 takes 58-93, emptying word 1; freeing the
+# second gives 64-93 back to word 1, which is not full, so the reference leaves
+# it unlisted and the single-item searches never see those 30 segments.
+HIDDEN_BY_RETURN = [("m", 34), ("m", 36), ("f", 1)]
+
+
+def runs_to_ops(steps):
+    """The serial trace (malloc sizes, 1<<63 | index frees) of a run list."""
+    ops, idx = [], []
+    for op, x in steps:
+        if op == "m":
+            idx.append(len(ops))
+            ops.append(x * SEG)
+        else:
+            ops.append((1 << 63) | idx[x])
+    return np.array(ops, dtype=np.uint64), idx
+
+
+def summary_lists_every_nonempty_word(sv):
+    top, bottom = int(sv.seg_tree_words[0]), sv.seg_tree_words[1:3]
+    return all(bool(top >> k & 1) == (int(w) != 0) for k, w in enumerate(bottom))
+
+
+@pytest.mark.parametrize("fixes,reachable", [
+    (PRODUCT_FIXES & ~FIX_RUN_RETURN_SUMMARY, 64),   # the reference: 30 segments unreachable
+    (PRODUCT_FIXES, 94),
+], ids=["reference", "product"])
+def test_a_returned_run_lists_every_word_it_refills(fixes, reachable):
+    o = Oracle(2 << 30, 42, fixes=fixes, boot=False)
+    got = replay_runs(o, HIDDEN_BY_RETURN)
+    assert [g // SEG for g in got] == [94, 58]
+    assert summary_lists_every_nonempty_word(o.export()) == (fixes == PRODUCT_FIXES)
+    singles = []
+    while (x := o.malloc(SEG)) != FAIL:
+        singles.append(x // SEG)
+    assert len(singles) == reachable and len(set(singles)) == reachable
+    assert not set(singles) & set(range(94, 128))
