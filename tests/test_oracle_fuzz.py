@@ -1,0 +1,100 @@
+"""Random request/free traces over every size tier (slices, 4 KiB-slice runs,
+whole blocks, segment runs) through the oracle with the product's fixes.
+
+Along the way each vEB tree (the segment tree and every per-class sub-tree,
+veb.cuh) keeps its summary exact: a summary bit is set exactly when the word
+below it is non-empty, which a serial trace must preserve (insert climbs from
+an empty word, remove from a word it empties, gather and return of a run
+update the words they touch).  Live requests never overlap and slices sit on
+their class boundary.  Freeing everything and trimming gives back a fresh
+allocator's trees.  In the reference's mode (FIX_RUN_RETURN_SUMMARY off) some
+of these seeds leave a word unlisted."""
+import numpy as np
+import pytest
+
+from gallatin_gb300._abi import FAIL
+from oracle.oracle import FIX_RUN_RETURN_SUMMARY, PRODUCT_FIXES, Oracle
+
+SEG = 16 << 20
+TREE_FIELDS = ["seg_tree_words", "sub_tree_words", "tree_ids", "slots", "free_counters"]
+
+
+def layer_words(universe):
+    """Words per layer, top first, as the tree lays them out (veb.cuh:541-576)."""
+    layers = (universe.bit_length() - 1) // 6 + 1
+    out, u = [], universe
+    for _ in range(layers):
+        u = (u - 1) // 64 + 1
+        out.insert(0, u)
+    return out
+
+
+def unlisted(words, universe):
+    """(layer, word) of the first summary bit that disagrees with its word."""
+    sizes = layer_words(universe)
+    offs = np.cumsum([0] + sizes)
+    assert offs[-1] == len(words)
+    for i in range(len(sizes) - 1):
+        up, lo = words[offs[i]:offs[i + 1]], words[offs[i + 1]:offs[i + 2]]
+        for k in range(len(lo)):
+            if bool(int(up[k // 64]) >> (k % 64) & 1) != (int(lo[k]) != 0):
+                return i + 1, k
+    return None
+
+
+def summaries_exact(o):
+    d = o.dims()
+    sv = o.export()
+    if unlisted(sv.seg_tree_words, d.num_segments):
+        return False
+    W = d.veb_words
+    return all(unlisted(sv.sub_tree_words[t * W:(t + 1) * W], d.num_segments) is None
+               for t in range(d.num_trees))
+
+
+def run_trace(seed, fixes, nops=1500):
+    rng = np.random.default_rng(seed)
+    o = Oracle([2 << 30, 4 << 30][seed % 2], 42, fixes=fixes, spares=bool(seed & 2))
+    fresh = o.export()
+    live = {}
+    for i in range(nops):
+        if live and rng.random() < 0.45:
+            off = list(live)[int(rng.integers(len(live)))]
+            o.free(off)
+            del live[off]
+            continue
+        t = rng.random()
+        if t < 0.4:
+            size = int(rng.integers(1, 4097))
+        elif t < 0.8:
+            size = int(rng.integers(32769, SEG + 1))
+        else:
+            size = int(rng.integers(SEG + 1, 8 * SEG))
+        off = o.malloc(size, smid=int(rng.integers(4)), tid=i)
+        if off != FAIL:
+            assert off not in live and off + size <= o.arena_bytes
+            if size <= 4096:
+                assert off % max(16, 1 << (size - 1).bit_length()) == 0
+            live[off] = size
+        if i % 10 == 0:
+            if not summaries_exact(o):
+                return False
+            spans = sorted(live.items())
+            assert all(a + n <= b for (a, n), (b, _) in zip(spans, spans[1:]))
+    for off in list(live):
+        o.free(off)
+    o.trim()
+    assert o.export().diff(fresh, fields=TREE_FIELDS) == []
+    return summaries_exact(o)
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_random_tiers_keep_summaries_exact_and_drain_to_fresh_trees(seed):
+    assert run_trace(seed, PRODUCT_FIXES)
+
+
+def test_the_reference_rule_leaves_words_unlisted():
+    """Seeds 3, 5, 9, 15, 22 and 23 of the same traces, with the reference's
+    return rule, list a non-empty word in no summary at some point."""
+    fixes = PRODUCT_FIXES & ~FIX_RUN_RETURN_SUMMARY
+    assert [s for s in range(24) if not run_trace(s, fixes)] == [3, 5, 9, 15, 22, 23]
