@@ -300,3 +300,21 @@ def test_a_returned_run_lists_every_word_it_refills(G):
         assert g.error_word() == 0
     finally:
         g.close()
+
+
+@pytest.mark.parametrize("seed", [3, 9])
+def test_tier_trace_matches_the_oracle(G, seed):
+    """1,500 serial requests over every tier (slices, blocks, segment runs)
+    with frees in random order: offsets and whole state equal the oracle's."""
+    from tests.test_oracle_fuzz import tier_trace
+    nbytes = [2 << 30, 4 << 30][seed % 2]
+    ops = tier_trace(seed)
+    g = G.Gallatin.generate_on_device(nbytes, 42)
+    try:
+        out, smid = g.replay(ops)
+        o = Oracle(nbytes, 42, fixes=PRODUCT_FIXES)
+        np.testing.assert_array_equal(out, o.replay(ops, smid=smid))
+        assert g.export().diff(o.export()) == []
+        assert g.error_word() == 0
+    finally:
+        g.close()

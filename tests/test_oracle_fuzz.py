@@ -98,3 +98,31 @@ def test_the_reference_rule_leaves_words_unlisted():
     return rule, list a non-empty word in no summary at some point."""
     fixes = PRODUCT_FIXES & ~FIX_RUN_RETURN_SUMMARY
     assert [s for s in range(24) if not run_trace(s, fixes)] == [3, 5, 9, 15, 22, 23]
+
+
+def tier_trace(seed, nops=1500):
+    """A serial trace (malloc sizes; 1<<63 | index frees of earlier mallocs not
+    yet freed) with the tier mix above, fixed before any replay."""
+    rng = np.random.default_rng(seed)
+    ops, open_ = [], []
+    for i in range(nops):
+        if open_ and rng.random() < 0.45:
+            ops.append((1 << 63) | open_.pop(int(rng.integers(len(open_)))))
+            continue
+        t = rng.random()
+        if t < 0.4:
+            ops.append(int(rng.integers(1, 4097)))
+        elif t < 0.8:
+            ops.append(int(rng.integers(32769, SEG + 1)))
+        else:
+            ops.append(int(rng.integers(SEG + 1, 8 * SEG)))
+        open_.append(i)
+    return np.array(ops, dtype=np.uint64)
+
+
+@pytest.mark.parametrize("seed", [3, 9])
+def test_tier_traces_replay_with_exact_summaries(seed):
+    o = Oracle([2 << 30, 4 << 30][seed % 2], 42, fixes=PRODUCT_FIXES)
+    out = o.replay(tier_trace(seed))
+    assert (out != FAIL).sum() > 500
+    assert summaries_exact(o)
