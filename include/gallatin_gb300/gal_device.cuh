@@ -427,8 +427,13 @@ GAL_DEVICE_COLD uint64_t veb_gather_multiple(const veb_ref &v, uint64_t n) {
     uint64_t hi = (lo + n - 1) / 64 + 1;
     lo = lo / 64;
     n = hi - lo;
-    for (uint64_t wb = lo; wb < lo + n; wb++)
-      if (ld_rlx(v.word(i + 1, wb)) == 0) amo_and(v.word(i, wb / 64), ~(1ULL << (wb % 64)));
+    for (uint64_t wb = lo; wb < lo + n; wb++) {
+      if (ld_rlx(v.word(i + 1, wb)) != 0) continue;
+      amo_and(v.word(i, wb / 64), ~(1ULL << (wb % 64)));
+      // an insert that refilled the word between the load and the clear found
+      // the summary bit still set and left it: put it back, as veb_remove does
+      if (ld_rlx(v.word(i + 1, wb)) != 0) amo_or(v.word(i, wb / 64), 1ULL << (wb % 64));
+    }
   }
   return found;
 }
