@@ -52,9 +52,10 @@ def summaries_exact(o):
                for t in range(d.num_trees))
 
 
-def run_trace(seed, fixes, nops=1500):
+def run_trace(seed, fixes, nops=1500, nbytes=None, max_run=8, every=10):
     rng = np.random.default_rng(seed)
-    o = Oracle([2 << 30, 4 << 30][seed % 2], 42, fixes=fixes, spares=bool(seed & 2))
+    nbytes = nbytes or [2 << 30, 4 << 30][seed % 2]
+    o = Oracle(nbytes, 42, fixes=fixes, spares=bool(seed & 2))
     fresh = o.export()
     live = {}
     for i in range(nops):
@@ -69,14 +70,14 @@ def run_trace(seed, fixes, nops=1500):
         elif t < 0.8:
             size = int(rng.integers(32769, SEG + 1))
         else:
-            size = int(rng.integers(SEG + 1, 8 * SEG))
+            size = int(rng.integers(SEG + 1, max_run * SEG))
         off = o.malloc(size, smid=int(rng.integers(4)), tid=i)
         if off != FAIL:
             assert off not in live and off + size <= o.arena_bytes
             if size <= 4096:
                 assert off % max(16, 1 << (size - 1).bit_length()) == 0
             live[off] = size
-        if i % 10 == 0:
+        if i % every == 0:
             if not summaries_exact(o):
                 return False
             spans = sorted(live.items())
@@ -98,6 +99,15 @@ def test_the_reference_rule_leaves_words_unlisted():
     return rule, list a non-empty word in no summary at some point."""
     fixes = PRODUCT_FIXES & ~FIX_RUN_RETURN_SUMMARY
     assert [s for s in range(24) if not run_trace(s, fixes)] == [3, 5, 9, 15, 22, 23]
+
+
+@pytest.mark.parametrize("fixes,exact", [(PRODUCT_FIXES, True),
+                                         (PRODUCT_FIXES & ~FIX_RUN_RETURN_SUMMARY, False)],
+                         ids=["product", "reference"])
+def test_three_layer_trees(fixes, exact):
+    """64 GiB = 4,096 segments: the trees have three layers, so claims and
+    returns of runs of up to 200 segments update two summary layers."""
+    assert run_trace(0, fixes, nops=2500, nbytes=64 << 30, max_run=200, every=250) == exact
 
 
 def tier_trace(seed, nops=1500):
