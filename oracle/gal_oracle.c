@@ -563,14 +563,17 @@ static int boot_block(orc_alloc *a, int tree, int smid, uint64_t tid) {
   return 0;
 }
 
-/* boot_shared_block_container_one_thread (gallatin.cuh:196-221) */
+/* boot_shared_block_container_one_thread (gallatin.cuh:196-221): every slot
+ * is tried even after one finds no block (the slot stays empty); the first
+ * failure is reported */
 int orc_boot_one_thread(orc_alloc *a) {
+  int first = 0;
   for (int tree = 0; tree < a->num_trees; tree++)
     for (int i = 0; i < a->nslots[tree]; i++) {
       int r = boot_block(a, tree, i, 0);
-      if (r) return r;
+      if (r && !first) first = r;
     }
-  return 0;
+  return first;
 }
 
 static void free_offset(orc_alloc *a, uint64_t offset);

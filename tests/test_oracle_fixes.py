@@ -89,3 +89,26 @@ def test_trim_keeps_live_allocations_out_of_reach():
     o.trim()
     after = o.export()
     assert not (set(after.slots.tolist()) & set(before.slots.tolist()) & live_blocks)
+
+
+def test_trim_on_a_full_arena_tries_every_slot():
+    """Boot and trim try every pinned slot even after one finds no block, as
+    the reference's one-thread boot does (gallatin.cuh:196-221): on a full
+    arena trim reports the failure, the slots it could not fill stay empty,
+    and once everything is freed another trim gives back the fresh trees."""
+    o = Oracle(1 << 30, 42)
+    fresh = o.export()
+    # a live slice in every pinned slot, so trim retires blocks it cannot
+    # return, then whole 1 MiB blocks until no segment is left
+    live = [o.malloc(16 << t, smid=i) for t in range(9) for i in range(128)]
+    assert FAIL not in live
+    while (x := o.malloc(1 << 20)) != FAIL:
+        live.append(x)
+    with pytest.raises(RuntimeError, match=r"trim failed \(-2\)"):
+        o.trim()
+    empty = int((o.export().slots == -1).sum())          # no block
+    assert 0 < empty < len(fresh.slots)
+    for x in live:
+        o.free(x)
+    o.trim()
+    assert o.export().diff(fresh, fields=TREE_FIELDS) == []
