@@ -136,3 +136,44 @@ def test_tier_traces_replay_with_exact_summaries(seed):
     out = o.replay(tier_trace(seed))
     assert (out != FAIL).sum() > 500
     assert summaries_exact(o)
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_trims_inside_a_trace_keep_live_requests_apart(seed):
+    """Trim at random points (a full arena leaves the slots it cannot fill
+    empty), one slot per SM or the reference's counts, with or without spare
+    blocks: live requests never overlap, summaries stay exact, and freeing
+    everything then trimming gives back the fresh trees."""
+    rng = np.random.default_rng(seed)
+    o = Oracle([1 << 30, 2 << 30][seed % 2], 42, spares=bool(seed & 2),
+               pinned_first=[128, 0][(seed >> 2) & 1])
+    fresh = o.export()
+    live = {}
+    for i in range(2000):
+        r = rng.random()
+        if r < 0.01:
+            try:
+                o.trim()
+            except RuntimeError:
+                pass                                   # arena full: some slots stay empty
+            continue
+        if live and r < 0.45:
+            off = list(live)[int(rng.integers(len(live)))]
+            o.free(off)
+            del live[off]
+            continue
+        size = int(rng.choice([rng.integers(1, 4097), rng.integers(4097, 32769),
+                               rng.integers(32769, SEG + 1), rng.integers(SEG + 1, 5 * SEG)],
+                              p=[0.6, 0.15, 0.2, 0.05]))
+        off = o.malloc(size, smid=int(rng.integers(152)), tid=i)
+        if off != FAIL:
+            assert off not in live
+            live[off] = size
+        if i % 50 == 0:
+            spans = sorted(live.items())
+            assert all(a + n <= b for (a, n), (b, _) in zip(spans, spans[1:]))
+            assert summaries_exact(o)
+    for off in list(live):
+        o.free(off)
+    o.trim()
+    assert o.export().diff(fresh, fields=TREE_FIELDS) == []
