@@ -123,7 +123,9 @@ def lib():
         "gal_bench_stamp": ([vp, u64, u64, C.c_int, vp, vp], C.c_int),
         "gal_bench_latency": ([vp, u64, u32, C.c_int, vp, vp], C.c_int),
         "gal_bench_atomic_peak": ([vp, vp], C.c_int),
+        "gal_bench_sector_probe": ([u32, u32, vp], C.c_int),
         "gal_job_launch": ([vp, u32, u64, u64, vp, vp, vp], C.c_int),
+        "gal_job_ctas": ([u32, u64], u32),
         "gal_bench_tables": ([vp, u32, vp, u64, C.c_int, vp, u32, vp, vp, u64, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
@@ -370,6 +372,13 @@ def churn_sizes(base_slot, n, seed):
     return out
 
 
+def sector_probe(hot, per_sector):
+    """Atomics/s on `hot` 8-byte counters packed per_sector to a 32-byte sector."""
+    a = C.c_double()
+    _check(lib().gal_bench_sector_probe(hot, per_sector, C.byref(a)), "gal_bench_sector_probe")
+    return a.value
+
+
 def atomic_peak():
     """(distinct-address, same-address) L2 atomicAdd.u32 rates in atomics/s."""
     a, b = C.c_double(), C.c_double()
@@ -404,6 +413,6 @@ def print_global_stats():
 
 __all__ = [
     "FAIL", "FREE_BIT", "GAL_POLICY_LOWEST", "GAL_POLICY_REFERENCE", "Gallatin", "GalError",
-    "StateView", "atomic_peak", "churn_sizes", "default_config", "free_global_allocator",
+    "StateView", "atomic_peak", "churn_sizes", "sector_probe", "default_config", "free_global_allocator",
     "global_allocator", "init_global_allocator", "lib", "print_global_stats",
 ]

@@ -25,6 +25,7 @@ GAL_DEV_ERR_BOOT = 0x40
 GAL_POLICY_REFERENCE = 0
 GAL_POLICY_LOWEST = 1
 GAL_ARENA_DEVICE, GAL_ARENA_HOST, GAL_ARENA_MANAGED = 0, 1, 2
+GAL_BLOCK_LAYOUT_DENSE, GAL_BLOCK_LAYOUT_RECORD = 0, 1
 
 GAL_MAX_TREES = 16
 GAL_MAX_VEB_LAYERS = 8
@@ -49,6 +50,7 @@ class GalConfig(C.Structure):
         ("arena_kind", C.c_uint32),
         ("spare_blocks", C.c_uint32),
         ("zero_fill", C.c_uint32),
+        ("block_layout", C.c_uint32),
     ]
 
 

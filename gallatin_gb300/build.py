@@ -22,6 +22,7 @@ HEADERS = [
     os.path.join(CSRC, "gal_batch.cuh"),
     os.path.join(CSRC, "churn.cuh"),
     os.path.join(CSRC, "workload.cuh"),
+    os.path.join(CSRC, "gal_internal.h"),
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include")]

@@ -4,6 +4,9 @@
 // reference build run literally the same request code.
 //
 // Alloc must provide  void* malloc(uint64_t)  and  void free(void*).
+// PAYLOAD = false gives the allocator-only form: the same requests, frees and
+// pointer stores, without the payload word written at malloc and checked at
+// free.
 #pragma once
 #include <stdint.h>
 
@@ -35,7 +38,7 @@ __device__ __forceinline__ void publish_live(uint32_t *live_bits, uint64_t slot,
   if ((threadIdx.x & 31) == 0) live_bits[slot >> 5] = b;
 }
 
-template <class Alloc>
+template <class Alloc, bool PAYLOAD = true>
 __device__ __forceinline__ void churn_malloc_body(Alloc *a, void **ptrs, uint32_t *live_bits,
                                                   uint64_t base, uint64_t n, uint32_t seed,
                                                   unsigned long long *stats) {
@@ -44,7 +47,7 @@ __device__ __forceinline__ void churn_malloc_body(Alloc *a, void **ptrs, uint32_
   uint64_t slot = base + tid;
   uint64_t size = mixed_size(slot, seed);
   void *p = a->malloc(size);
-  if (p) *(volatile uint32_t *)p = payload(slot, seed);
+  if (PAYLOAD && p) *(volatile uint32_t *)p = payload(slot, seed);
   ptrs[slot] = p;
   publish_live(live_bits, slot, p != nullptr);
   warp_count(&stats[0], p != nullptr);
@@ -157,6 +160,7 @@ __device__ __forceinline__ uint32_t list_selected(uint32_t *live_bits, uint64_t 
 
 // Pointers and payload words of list entries j0 + k*32 + lane (k < FREE_SLOTS),
 // loads issued together; go[k] marks the entries that exist.
+template <bool PAYLOAD = true>
 __device__ __forceinline__ void load_listed(void **ptrs, uint64_t w0, const uint16_t *list,
                                             uint32_t total, uint32_t j0, uint32_t seed, void **p,
                                             bool *go, uint32_t &nbad, uint32_t &ngo) {
@@ -172,17 +176,17 @@ __device__ __forceinline__ void load_listed(void **ptrs, uint64_t w0, const uint
 #pragma unroll
   for (int k = 0; k < FREE_SLOTS; k++) {
     go[k] = p[k] != nullptr;
-    seen[k] = go[k] ? *(const uint32_t *)p[k] : 0u;
+    seen[k] = PAYLOAD && go[k] ? *(const uint32_t *)p[k] : 0u;
   }
 #pragma unroll
   for (int k = 0; k < FREE_SLOTS; k++)
     if (go[k]) {
-      nbad += seen[k] != payload(slot[k], seed);
+      if (PAYLOAD) nbad += seen[k] != payload(slot[k], seed);
       ngo++;
     }
 }
 
-template <class Alloc>
+template <class Alloc, bool PAYLOAD = true>
 __device__ __forceinline__ void churn_free_warps(Alloc *a, void **ptrs, uint32_t *live_bits,
                                                  uint64_t nslots, uint32_t round, uint32_t seed,
                                                  bool all, unsigned long long *stats,
@@ -196,7 +200,7 @@ __device__ __forceinline__ void churn_free_warps(Alloc *a, void **ptrs, uint32_t
     for (uint32_t j0 = 0; j0 < total; j0 += 32u * FREE_SLOTS) {
       void *p[FREE_SLOTS];
       bool go[FREE_SLOTS];
-      load_listed(ptrs, w0, list, total, j0, seed, p, go, nbad, ngo);
+      load_listed<PAYLOAD>(ptrs, w0, list, total, j0, seed, p, go, nbad, ngo);
       free_many<Alloc>::run(a, p, go);
     }
     __syncwarp();

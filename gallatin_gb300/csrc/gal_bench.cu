@@ -54,20 +54,49 @@ namespace {
 
 constexpr int BT = 512;  // batched CTA size
 
+template <bool PAYLOAD>
 __global__ void k_churn_malloc_plain(const gal::state *s, void **ptrs, uint32_t *live, uint64_t base,
                                      uint64_t n, uint32_t seed, unsigned long long *stats) {
   plain_alloc a{s};
-  galwl::churn_malloc_body(&a, ptrs, live, base, n, seed, stats);
+  galwl::churn_malloc_body<plain_alloc, PAYLOAD>(&a, ptrs, live, base, n, seed, stats);
 }
 
 constexpr int FREE_BT = 256;  // free phase CTA size (persistent grid)
 
+template <bool PAYLOAD>
 __global__ void __launch_bounds__(FREE_BT)
     k_churn_free_plain(const gal::state *s, void **ptrs, uint32_t *live, uint64_t nslots,
                        uint32_t round, uint32_t seed, int all, unsigned long long *stats) {
   __shared__ uint16_t lists[FREE_BT / 32][galwl::WARP_SLOTS];
   plain_alloc a{s};
-  galwl::churn_free_warps(&a, ptrs, live, nslots, round, seed, all != 0, stats, lists[threadIdx.x >> 5]);
+  galwl::churn_free_warps<plain_alloc, PAYLOAD>(&a, ptrs, live, nslots, round, seed, all != 0, stats,
+                                                lists[threadIdx.x >> 5]);
+}
+
+// persistent malloc phase of one round through the CTA reservoirs
+// (gal::res_malloc): each thread serves slots c + threadIdx.x of the CTA's
+// chunks, so a warp's lanes keep 32 consecutive slots for the liveness words
+constexpr int RES_BT = 256;
+template <bool PAYLOAD>
+__global__ void __launch_bounds__(RES_BT)
+    k_churn_malloc_res(const gal::state *s, void **ptrs, uint32_t *live, uint64_t base, uint64_t n,
+                       uint32_t seed, uint32_t run, unsigned long long *stats) {
+  __shared__ gal::cta_res_smem sm;
+  gal::cta_res_init(sm, run);
+  __syncthreads();
+  for (uint64_t c = (uint64_t)blockIdx.x * RES_BT; c < n; c += (uint64_t)gridDim.x * RES_BT) {
+    const uint64_t t = c + threadIdx.x;
+    if (t >= n) break;  // whole warps: n is a multiple of SLOT_ALIGN
+    const uint64_t slot = base + t;
+    void *p = gal::res_malloc(s, galwl::mixed_size(slot, seed), sm);
+    if (PAYLOAD && p) *(volatile uint32_t *)p = galwl::payload(slot, seed);
+    ptrs[slot] = p;
+    galwl::publish_live(live, slot, p != nullptr);
+    galwl::warp_count(&stats[0], p != nullptr);
+    galwl::warp_count(&stats[1], p == nullptr);
+  }
+  __syncthreads();
+  gal::cta_res_release(s, sm);
 }
 
 // persistent, CTA-aggregated malloc phase of one round: BW worker threads and
@@ -247,6 +276,27 @@ __global__ void __launch_bounds__(BT)
   gal::cta_workers_done(sm);
 }
 
+__global__ void __launch_bounds__(RES_BT)
+    k_lat_malloc_res(const gal::state *s, void **ptrs, uint64_t base, uint64_t n, uint32_t seed,
+                     uint32_t *cycles) {
+  __shared__ gal::cta_res_smem sm;
+  gal::cta_res_init(sm, 128);
+  __syncthreads();
+  for (uint64_t c = (uint64_t)blockIdx.x * RES_BT; c < n; c += (uint64_t)gridDim.x * RES_BT) {
+    const uint64_t t = c + threadIdx.x;
+    if (t >= n) break;
+    const uint64_t size = galwl::mixed_size(base + t, seed);
+    long long c0 = clock64();
+    void *p = gal::res_malloc(s, size, sm);
+    long long c1 = clock64();
+    if (p) *(volatile uint32_t *)p = galwl::payload(base + t, seed);
+    ptrs[base + t] = p;
+    cycles[t] = (uint32_t)min(c1 - c0, 0xFFFFFFFFll);
+  }
+  __syncthreads();
+  gal::cta_res_release(s, sm);
+}
+
 // the batched free path (gal_free_batched): warp teams per block through
 // gal::free_n, here one pointer per thread so each free is timed alone
 __global__ void __launch_bounds__(BT)
@@ -280,12 +330,31 @@ __global__ void k_atomic_probe(uint32_t *buf, uint64_t words, int iters, int sam
   if (acc == 0xFFFFFFFFu) sink[0] = acc;
 }
 
+// Hot-word layout probe: `hot` counters of 8 bytes, `per_sector` of them in
+// each 32-byte sector (1 = one counter per sector, 4 = densely packed); warp w
+// of the grid adds to counter w % hot with one lane, `iters` times, so every
+// counter is hit by its own warps only, as a pinned block's malloc word is hit
+// by the claims of its SM.
+__global__ void k_sector_probe(unsigned long long *buf, uint32_t hot, uint32_t per_sector, int iters,
+                               unsigned long long *sink) {
+  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if ((threadIdx.x & 31) != 0) return;
+  const uint32_t w = (uint32_t)(warp % hot);
+  unsigned long long *p = buf + (uint64_t)(w / per_sector) * 4 + (w % per_sector);
+  unsigned long long acc = 0;
+  for (int k = 0; k < iters; k++) acc += atomicAdd(p, 1ull);
+  if (acc == ~0ull) sink[0] = acc;
+}
+
 struct churn_ctx {
   gal_handle *h;
   const gal::state *d;
   uint64_t N;
   uint32_t R, seed;
   int batched;
+  bool payload;   // false: the allocator-only form (no payload written or checked)
+  uint32_t run;   // reservoir run length (slices)
+  int grid_r;     // persistent grid of the reservoir malloc
   void **ptrs;
   uint32_t *live;  // slot liveness bits (churn.cuh)
   unsigned long long *stats;
@@ -324,15 +393,27 @@ void enqueue_step(churn_ctx &c, cudaStream_t st, bool capturing) {
       } else {
         const uint64_t chunk = (uint64_t)(FREE_BT / 32) * galwl::WARP_SLOTS;
         unsigned g = (unsigned)std::min<uint64_t>((nscan + chunk - 1) / chunk, (uint64_t)c.grid_f);
-        k_churn_free_plain<<<g, FREE_BT, 0, st>>>(c.d, c.ptrs, c.live, nscan, r, c.seed, drain ? 1 : 0,
-                                                 c.stats);
+        if (c.payload)
+          k_churn_free_plain<true><<<g, FREE_BT, 0, st>>>(c.d, c.ptrs, c.live, nscan, r, c.seed,
+                                                         drain ? 1 : 0, c.stats);
+        else
+          k_churn_free_plain<false><<<g, FREE_BT, 0, st>>>(c.d, c.ptrs, c.live, nscan, r, c.seed,
+                                                          drain ? 1 : 0, c.stats);
       }
       mark(1, false);
     }
     if (drain) break;
     uint64_t base = c.N * r;
     mark(0, true);
-    if (c.batched & 1) {
+    if (c.batched & 4) {
+      const unsigned gr = (unsigned)std::min<uint64_t>((c.N + RES_BT - 1) / RES_BT, (uint64_t)c.grid_r);
+      if (c.payload)
+        k_churn_malloc_res<true><<<gr, RES_BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.run,
+                                                       c.stats);
+      else
+        k_churn_malloc_res<false><<<gr, RES_BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.run,
+                                                        c.stats);
+    } else if (c.batched & 1) {
       const int per = 1 << c.k_shift;  // requests per thread per iteration
       unsigned gk = (unsigned)std::min<uint64_t>((c.N + (uint64_t)BW * per - 1) / ((uint64_t)BW * per),
                                                  (uint64_t)c.grid_b);
@@ -342,9 +423,12 @@ void enqueue_step(churn_ctx &c, cudaStream_t st, bool capturing) {
         k_churn_malloc_batched<2><<<gk, BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats);
       else
         k_churn_malloc_batched<1><<<gk, BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats);
+    } else if (c.payload) {
+      k_churn_malloc_plain<true><<<(unsigned)((c.N + 255) / 256), 256, 0, st>>>(c.d, c.ptrs, c.live, base,
+                                                                              c.N, c.seed, c.stats);
     } else {
-      k_churn_malloc_plain<<<(unsigned)((c.N + 255) / 256), 256, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed,
-                                                                        c.stats);
+      k_churn_malloc_plain<false><<<(unsigned)((c.N + 255) / 256), 256, 0, st>>>(c.d, c.ptrs, c.live, base,
+                                                                               c.N, c.seed, c.stats);
     }
     mark(0, false);
   }
@@ -368,10 +452,13 @@ extern "C" {
 /* Mixed-size churn.  One step = `rounds` x (coin frees of the live slots before
  * every round but the first, then threads_per_round mallocs), then a drain of
  * all live slots; every step serves the same requests.  batched: bit 0 CTA-aggregated
- * malloc, bit 1 CTA-aggregated free (else per-thread with warp teams), bits 4-5:
- * log2 of the requests each thread of the CTA-aggregated malloc serves per
- * iteration (0-2); CTA-aggregated persistent kernels; use_graph: the step is one
- * captured CUDA graph.
+ * malloc, bit 1 CTA-aggregated free (else per-thread with warp teams), bit 2
+ * malloc through the CTA reservoirs (gal::res_malloc; takes precedence over
+ * bit 0), bit 3 the allocator-only form (no payload written or checked),
+ * bits 4-5: log2 of the requests each thread of the CTA-aggregated malloc
+ * serves per iteration (0-2), bits 8-11: log2 of the reservoir run length
+ * (0: 128 slices); persistent kernels; use_graph: the step is one captured
+ * CUDA graph.
  * step_ms[i]: duration of timed step i (CUDA events on the launching stream). */
 int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, uint32_t seed,
                     int batched, int use_graph, int warmup, int steps, float *step_ms,
@@ -385,9 +472,15 @@ int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, 
   c.N = threads_per_round;
   c.R = rounds;
   c.seed = seed;
-  c.batched = batched & 3;
+  c.batched = batched & 7;
+  c.payload = !(batched & 8);
   c.k_shift = (batched >> 4) & 3;
   if (c.k_shift > 2) return GAL_ERR_ARGS;
+  {
+    const int lr = (batched >> 8) & 15;
+    c.run = lr ? 1u << lr : 128u;
+    if (c.run > gal::SLICES_PER_BLOCK) return GAL_ERR_ARGS;
+  }
   c.ptrs = nullptr;
   c.live = nullptr;
   c.stats = nullptr;
@@ -403,8 +496,11 @@ int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, 
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_churn_malloc_batched<1>, BT, 0);
   c.grid_b = sms * (per_sm > 0 ? per_sm : 1);
   per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_churn_free_plain, FREE_BT, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_churn_free_plain<true>, FREE_BT, 0);
   c.grid_f = sms * (per_sm > 0 ? per_sm : 1);
+  per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_churn_malloc_res<true>, RES_BT, 0);
+  c.grid_r = sms * (per_sm > 0 ? per_sm : 1);
   c.ev.resize(2 * nkern);
   c.kind.resize(nkern);
   CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
@@ -665,7 +761,9 @@ done:
 
 /* Per-request latency in SM cycles (clock64) of one churn round of n mixed
  * requests at full concurrency: malloc_cycles[i], then free_cycles[i] when the
- * same allocations are freed.  One unmeasured round first.  Host buffers. */
+ * same allocations are freed.  One unmeasured round first.  Host buffers.
+ * batched: 0 per-thread calls, 1 CTA-aggregated claims and batched frees,
+ * 2 the CTA reservoirs and batched frees. */
 int gal_bench_latency(gal_handle *h, uint64_t n, uint32_t seed, int batched,
                       uint32_t *malloc_cycles, uint32_t *free_cycles) {
   if (!h || !n || !malloc_cycles || !free_cycles) return GAL_ERR_ARGS;
@@ -678,12 +776,18 @@ int gal_bench_latency(gal_handle *h, uint64_t n, uint32_t seed, int batched,
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lat_malloc_batched, BT, 0);
   unsigned gb = (unsigned)std::min<uint64_t>((n + BW - 1) / BW, (uint64_t)sms * (per_sm > 0 ? per_sm : 1));
+  per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lat_malloc_res, RES_BT, 0);
+  unsigned gr = (unsigned)std::min<uint64_t>((n + RES_BT - 1) / RES_BT, (uint64_t)sms * (per_sm > 0 ? per_sm : 1));
   unsigned gp = (unsigned)((n + 255) / 256);
   CK(cudaMalloc(&ptrs, n * sizeof(void *)));
   CK(cudaMalloc(&cm, n * 4));
   CK(cudaMalloc(&cf, n * 4));
   for (int r = 0; r < 2; r++) {
-    if (batched) {
+    if (batched == 2) {
+      k_lat_malloc_res<<<gr, RES_BT>>>(d, ptrs, 0, n, seed + r, cm);
+      k_lat_free_batched<<<gb, BT>>>(d, ptrs, 0, n, cf);
+    } else if (batched) {
       k_lat_malloc_batched<<<gb, BT>>>(d, ptrs, 0, n, seed + r, cm);
       k_lat_free_batched<<<gb, BT>>>(d, ptrs, 0, n, cf);
     } else {
@@ -748,6 +852,48 @@ done:
   if (c) cudaEventDestroy(c);
   if (ptrs) cudaFree(ptrs);
   if (stats) cudaFree(stats);
+  return rc;
+}
+
+/* Atomics per second on `hot` 8-byte counters packed `per_sector` to a
+ * 32-byte sector (1, 2 or 4), each counter hit by warps of its own
+ * (k_sector_probe): how the packing of concurrently claimed malloc words
+ * changes the L2 atomic rate. */
+int gal_bench_sector_probe(uint32_t hot, uint32_t per_sector, double *atomics_per_s) {
+  if (!atomics_per_s || !hot || !per_sector || per_sector > 4) return GAL_ERR_ARGS;
+  int rc = GAL_OK;
+  unsigned long long *buf = nullptr, *sink = nullptr;
+  cudaEvent_t a = nullptr, b = nullptr;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const unsigned block = 256, grid = (unsigned)sms * 4;
+  const int iters = 512;
+  const uint64_t words = ((uint64_t)hot / per_sector + 1) * 4;
+  CK(cudaMalloc(&buf, words * 8));
+  CK(cudaMalloc(&sink, 8));
+  CK(cudaMemset(buf, 0, words * 8));
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  {
+    float best = 1e30f;
+    for (int rep = 0; rep < 5; rep++) {
+      CK(cudaEventRecord(a));
+      k_sector_probe<<<grid, block>>>(buf, hot, per_sector, iters, sink);
+      CK(cudaEventRecord(b));
+      CK(cudaEventSynchronize(b));
+      CK(cudaGetLastError());
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, a, b));
+      if (rep > 0 && ms < best) best = ms;
+    }
+    *atomics_per_s = (double)grid * (block / 32) * iters / (best * 1e-3);
+  }
+done:
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  if (buf) cudaFree(buf);
+  if (sink) cudaFree(sink);
   return rc;
 }
 

@@ -9,10 +9,12 @@
 
 #include <mutex>
 #include <unordered_map>
+#include <vector>
 
 #include "../../include/gallatin_gb300.h"
 #include "../../include/gallatin_gb300/gal_device.cuh"
 #include "gal_batch.cuh"
+#include "gal_internal.h"
 
 struct gal_handle {
   int device = 0;
@@ -50,11 +52,15 @@ uint32_t log2u(uint64_t x) { return 63 - __builtin_clzll(x); }
 size_t align_up(size_t x, size_t a) { return (x + a - 1) & ~(a - 1); }
 
 // ---------------------------------------------------------------- kernels
-__global__ void k_init_words(unsigned long long *mwords, uint64_t nblocks, uint64_t *seg_tree,
-                             gal::veb_shape sh) {
+// malloc words 4097 (Block::init), every segment's count -1 in generation 0,
+// the segment tree full; everything else was zeroed
+__global__ void k_init_words(gal::state st, uint64_t nblocks) {
+  uint64_t *seg_tree = st.seg_tree;
+  const gal::veb_shape &sh = st.veb;
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t b = i; b < nblocks; b += stride) mwords[b] = 4097ull;  // Block::init
+  for (uint64_t b = i; b < nblocks; b += stride) *gal::mword_ptr(&st, (uint32_t)b) = 4097ull;
+  for (uint64_t g = i; g < st.num_segments; g += stride) st.act[g] = gal::act_word(0, -1);
   for (uint32_t l = 0; l < sh.layers; l++) {
     uint64_t items = sh.items[l];
     for (uint64_t w = i; w < sh.nwords[l]; w += stride) {
@@ -82,7 +88,7 @@ __global__ void k_trim(const gal::state *s) {
   for (uint32_t i = 0; i < s->total_slots; i++) {  // spare blocks: nothing handed out
     uint32_t blk = atomicExch(s->spares + i, gal::NOBLK);
     if (blk == gal::NOBLK) continue;
-    unsigned long long old = atomicAdd(&s->mwords[blk], (unsigned long long)gal::SLICES_PER_BLOCK);
+    unsigned long long old = atomicAdd(gal::mword_ptr(s, blk), (unsigned long long)gal::SLICES_PER_BLOCK);
     uint32_t handed_out = (uint32_t)old;
     if (handed_out < gal::SLICES_PER_BLOCK) gal::credit_frees(s, blk, gal::SLICES_PER_BLOCK - handed_out);
   }
@@ -90,7 +96,7 @@ __global__ void k_trim(const gal::state *s) {
     for (uint32_t i = 0; i < s->slot_count[t]; i++) {
       uint32_t blk = atomicExch(s->slots + s->slot_base[t] + i, gal::NOBLK);
       if (blk == gal::NOBLK) continue;
-      unsigned long long old = atomicAdd(&s->mwords[blk], (unsigned long long)gal::SLICES_PER_BLOCK);
+      unsigned long long old = atomicAdd(gal::mword_ptr(s, blk), (unsigned long long)gal::SLICES_PER_BLOCK);
       uint32_t handed_out = (uint32_t)old;
       if (handed_out < gal::SLICES_PER_BLOCK) gal::credit_frees(s, blk, gal::SLICES_PER_BLOCK - handed_out);
     }
@@ -99,13 +105,10 @@ __global__ void k_trim(const gal::state *s) {
   for (uint64_t seg = 0; seg < s->num_segments; seg++) {
     uint16_t tree = s->tree_ids[seg];
     if (tree >= s->num_trees) continue;
-    int idle = (int)gal::blocks_in_segment(s, tree) - 1;
-    if (atomicCAS(&s->active[seg], idle, -1) != idle) continue;
-    gal::veb_remove(gal::sub_tree(s, tree), seg);
-    __threadfence();
-    if (gal::cas16(&s->tree_ids[seg], tree, gal::FREE_TREE) != tree) gal::set_error(s, GAL_DEV_ERR_SEGMENT_SETUP);
-    __threadfence();
-    gal::veb_insert(gal::seg_tree(s), seg);
+    const uint32_t nb = gal::blocks_in_segment(s, tree);
+    const unsigned long long w = s->act[seg];
+    if (gal::act_count(w) != (int32_t)nb - 1) continue;
+    gal::release_segment(s, seg, tree, gal::act_gen(w), nb);
   }
   for (uint32_t t = 0; t < s->num_trees; t++)
     for (uint32_t i = 0; i < s->slot_count[t]; i++)
@@ -115,17 +118,14 @@ __global__ void k_trim(const gal::state *s) {
 __global__ void k_export_blocks(const gal::state *s, uint32_t *mc, uint64_t nblocks) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t b = i; b < nblocks; b += stride) {
-    unsigned long long w = s->mwords[b];
-    mc[b] = (uint32_t)(((w >> 32) << 20) + (w & 0xFFFFFFFFull));  // reference packing
-  }
+  for (uint64_t b = i; b < nblocks; b += stride) mc[b] = gal::export_mword(s, (uint32_t)b);
 }
 
 __global__ void k_import_blocks(const gal::state *s, const uint32_t *mc, uint64_t nblocks) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t b = i; b < nblocks; b += stride)
-    s->mwords[b] = ((unsigned long long)(mc[b] >> 20) << 32) | (mc[b] & 0xFFFFFu);
+    *gal::mword_ptr(s, (uint32_t)b) = ((unsigned long long)(mc[b] >> 20) << 32) | (mc[b] & 0xFFFFFu);
 }
 
 __global__ void k_stats(const gal::state *s, gal_stats *out) {
@@ -146,7 +146,7 @@ __global__ void k_stats(const gal::state *s, gal_stats *out) {
     uint16_t id = s->tree_ids[g];
     if (id < T) {
       atomicAdd(&acc[3 + id], 1ull);
-      int handed = (int)gal::blocks_in_segment(s, id) - 1 - s->active[g];
+      int handed = (int)gal::blocks_in_segment(s, id) - 1 - gal::act_count(s->act[g]);
       if (handed > 0) atomicAdd(&acc[3 + 2 * GAL_MAX_TREES + id], (unsigned long long)handed);
     } else if (id != 0xFFFF && id > T) {
       atomicAdd(&acc[1], 1ull);
@@ -349,7 +349,7 @@ int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot
   if (cfg.subtree_policy > GAL_POLICY_LOWEST) return GAL_ERR_ARGS;
   if (cfg.team_width > 32 || (cfg.team_width & (cfg.team_width - 1))) return GAL_ERR_ARGS;
   if (cfg.arena_kind > GAL_ARENA_MANAGED) return GAL_ERR_ARGS;
-  if (cfg.spare_blocks > 1 || cfg.zero_fill > 1) return GAL_ERR_ARGS;
+  if (cfg.spare_blocks > 1 || cfg.zero_fill > 1 || cfg.block_layout > 1) return GAL_ERR_ARGS;
   const uint32_t T = log2u(cfg.max_size) - log2u(cfg.min_size) + 1;
   const uint64_t S = num_bytes / cfg.bytes_per_segment;
   if (T > GAL_MAX_TREES || S == 0 || S + T + 1 >= 0xFFFF) return GAL_ERR_ARGS;
@@ -424,11 +424,15 @@ int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot
   size_t o_seg = carve((size_t)st.veb.words * 8);
   size_t o_sub = carve((size_t)T * st.veb.words * 8);
   size_t o_ids = carve(S * 2);
-  size_t o_act = carve(S * 4), o_qc = carve(S * 4), o_qfc = carve(S * 4), o_fqfc = carve(S * 4);
-  size_t o_mw = carve(nblocks * 8), o_fc = carve(nblocks * 4), o_q = carve(nblocks * 4);
+  size_t o_act = carve(S * 8), o_qc = carve(S * 4), o_qfc = carve(S * 4), o_fqfc = carve(S * 4);
+  // block counters: one 32-byte record per block, or two dense arrays
+  const bool records = cfg.block_layout == GAL_BLOCK_LAYOUT_RECORD;
+  size_t o_mw = carve(nblocks * (records ? gal::BLOCK_RECORD_BYTES : 8));
+  size_t o_fc = records ? o_mw + 8 : carve(nblocks * 4);
+  size_t o_q = carve(nblocks * 4);
   size_t o_slots = carve(total * 4);
   size_t o_spares = carve(total * 4);
-  size_t o_locks = carve(128), o_err = carve(128);
+  size_t o_locks = carve((size_t)(T + 1) * gal::LOCK_STRIDE * 4), o_err = carve(128);
   h->meta_bytes = off;
   if (cudaMalloc(&h->meta, h->meta_bytes) != cudaSuccess) {
     free_handle(h);
@@ -445,12 +449,14 @@ int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot
   st.seg_tree = (uint64_t *)(m + o_seg);
   st.sub_trees = (uint64_t *)(m + o_sub);
   st.tree_ids = (uint16_t *)(m + o_ids);
-  st.active = (int32_t *)(m + o_act);
+  st.act = (unsigned long long *)(m + o_act);
   st.qc = (uint32_t *)(m + o_qc);
   st.qfc = (uint32_t *)(m + o_qfc);
   st.fqfc = (uint32_t *)(m + o_fqfc);
   st.mwords = (unsigned long long *)(m + o_mw);
   st.fctr = (uint32_t *)(m + o_fc);
+  st.mstride = records ? gal::BLOCK_RECORD_BYTES / 8 : 1;
+  st.fstride = records ? gal::BLOCK_RECORD_BYTES / 4 : 1;
   st.queues = (uint32_t *)(m + o_q);
   st.slots = (uint32_t *)(m + o_slots);
   st.spares = (uint32_t *)(m + o_spares);
@@ -463,11 +469,10 @@ int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot
     // everything zero, then the non-zero patterns
     if (cudaMemset(h->meta, 0, h->meta_bytes) != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
     if (cudaMemset(st.tree_ids, 0xFF, S * 2) != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
-    if (cudaMemset(st.active, 0xFF, S * 4) != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
     if (cudaMemset(st.queues, 0xFF, nblocks * 4) != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
     if (cudaMemset(st.slots, 0xFF, total * 4) != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
     if (cudaMemset(st.spares, 0xFF, total * 4) != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
-    k_init_words<<<1024, 256>>>(st.mwords, nblocks, st.seg_tree, st.veb);
+    k_init_words<<<1024, 256>>>(st, nblocks);
     if (cudaGetLastError() != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
     if (cfg.zero_arena && cudaMemset(h->arena, 0, h->arena_bytes) != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
     if (cudaMemcpy(h->d_state, &st, sizeof(st), cudaMemcpyHostToDevice) != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
@@ -476,6 +481,9 @@ int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot
       if (cudaGetLastError() != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
     }
     if (cudaDeviceSynchronize() != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
+    // the allocation-free export's fixed array and stream, placed now so that
+    // the export itself never loads or allocates anything
+    if (gal_noalloc_setup(h->device) != GAL_OK) { rc = GAL_ERR_CUDA; break; }
     uint32_t err = 0;
     if (cudaMemcpy(&err, st.error, 4, cudaMemcpyDeviceToHost) != cudaSuccess) { rc = GAL_ERR_CUDA; break; }
     if (err) { rc = GAL_ERR_DEVICE; break; }
@@ -548,6 +556,7 @@ int gal_config_default(gal_config *cfg) {
   cfg->arena_kind = GAL_ARENA_DEVICE;
   cfg->spare_blocks = 0;
   cfg->zero_fill = 0;
+  cfg->block_layout = GAL_BLOCK_LAYOUT_RECORD;
   return GAL_OK;
 }
 
@@ -638,32 +647,38 @@ int gal_state_dims_get(gal_handle *h, gal_state_dims *out) {
   return GAL_OK;
 }
 
-int gal_export_state(gal_handle *h, const gal_state_view *v) {
+int gal_export_state(gal_handle *h, gal_state_view *v) {
   if (!h || !v) return GAL_ERR_ARGS;
   const gal::state &st = h->st;
   const uint64_t S = st.num_segments, nb = S << st.bps_shift, W = st.veb.words, T = st.num_trees;
+  gal_device_guard on_dev(h->device);
+  CUDA_TRY(on_dev.err);
   CUDA_TRY(cudaDeviceSynchronize());
-  CUDA_TRY(cudaMemcpy(v->seg_tree_words, st.seg_tree, W * 8, cudaMemcpyDeviceToHost));
-  CUDA_TRY(cudaMemcpy(v->sub_tree_words, st.sub_trees, T * W * 8, cudaMemcpyDeviceToHost));
-  CUDA_TRY(cudaMemcpy(v->tree_ids, st.tree_ids, S * 2, cudaMemcpyDeviceToHost));
-  CUDA_TRY(cudaMemcpy(v->active_counts, st.active, S * 4, cudaMemcpyDeviceToHost));
-  CUDA_TRY(cudaMemcpy(v->queue_counters, st.qc, S * 4, cudaMemcpyDeviceToHost));
-  CUDA_TRY(cudaMemcpy(v->queue_free_counters, st.qfc, S * 4, cudaMemcpyDeviceToHost));
-  CUDA_TRY(cudaMemcpy(v->final_queue_free_counters, st.fqfc, S * 4, cudaMemcpyDeviceToHost));
-  CUDA_TRY(cudaMemcpy(v->free_counters, st.fctr, nb * 4, cudaMemcpyDeviceToHost));
-  CUDA_TRY(cudaMemcpy(v->queues, st.queues, nb * 4, cudaMemcpyDeviceToHost));
-  CUDA_TRY(cudaMemcpy(v->slots, st.slots, (uint64_t)st.total_slots * 4, cudaMemcpyDeviceToHost));
+  const cudaMemcpyKind D2H = cudaMemcpyDeviceToHost;
+  CUDA_TRY(cudaMemcpy(v->seg_tree_words, st.seg_tree, W * 8, D2H));
+  CUDA_TRY(cudaMemcpy(v->sub_tree_words, st.sub_trees, T * W * 8, D2H));
+  CUDA_TRY(cudaMemcpy(v->tree_ids, st.tree_ids, S * 2, D2H));
+  CUDA_TRY(cudaMemcpy2D(v->active_counts, 4, st.act, 8, 4, S, D2H));  // low halves: biased counts
+  CUDA_TRY(cudaMemcpy(v->queue_counters, st.qc, S * 4, D2H));
+  CUDA_TRY(cudaMemcpy(v->queue_free_counters, st.qfc, S * 4, D2H));
+  CUDA_TRY(cudaMemcpy(v->final_queue_free_counters, st.fqfc, S * 4, D2H));
+  CUDA_TRY(cudaMemcpy2D(v->free_counters, 4, st.fctr, (size_t)st.fstride * 4, 4, nb, D2H));
+  CUDA_TRY(cudaMemcpy(v->queues, st.queues, nb * 4, D2H));
+  CUDA_TRY(cudaMemcpy(v->slots, st.slots, (uint64_t)st.total_slots * 4, D2H));
   uint32_t *d_mc = nullptr;
   CUDA_TRY(cudaMalloc(&d_mc, nb * 4));
   k_export_blocks<<<1024, 256>>>(h->d_state, d_mc, nb);
-  cudaError_t e = cudaMemcpy(v->malloc_counters, d_mc, nb * 4, cudaMemcpyDeviceToHost);
+  cudaError_t e = cudaMemcpy(v->malloc_counters, d_mc, nb * 4, D2H);
   cudaFree(d_mc);
   if (e != cudaSuccess) return GAL_ERR_CUDA;
-  uint32_t locks = 0, err = 0;
-  CUDA_TRY(cudaMemcpy(&locks, st.locks, 4, cudaMemcpyDeviceToHost));
-  CUDA_TRY(cudaMemcpy(&err, st.error, 4, cudaMemcpyDeviceToHost));
-  ((gal_state_view *)v)->locks = locks;
-  ((gal_state_view *)v)->error_word = err;
+  uint32_t locks[GAL_MAX_TREES + 1] = {}, err = 0;
+  CUDA_TRY(cudaMemcpy2D(locks, 4, st.locks, gal::LOCK_STRIDE * 4, 4, T + 1, D2H));
+  CUDA_TRY(cudaMemcpy(&err, st.error, 4, D2H));
+  for (uint64_t i = 0; i < S; i++) v->active_counts[i] = gal::act_unbias((uint32_t)v->active_counts[i]);
+  uint32_t bits = 0;
+  for (uint32_t t = 0; t <= T; t++) bits |= locks[t] ? 1u << t : 0u;
+  v->locks = bits;
+  v->error_word = err;
   return GAL_OK;
 }
 
@@ -671,29 +686,37 @@ int gal_import_state(gal_handle *h, const gal_state_view *v) {
   if (!h || !v) return GAL_ERR_ARGS;
   const gal::state &st = h->st;
   const uint64_t S = st.num_segments, nb = S << st.bps_shift, W = st.veb.words, T = st.num_trees;
+  gal_device_guard on_dev(h->device);
+  CUDA_TRY(on_dev.err);
   CUDA_TRY(cudaDeviceSynchronize());
-  CUDA_TRY(cudaMemcpy(st.seg_tree, v->seg_tree_words, W * 8, cudaMemcpyHostToDevice));
-  CUDA_TRY(cudaMemcpy(st.sub_trees, v->sub_tree_words, T * W * 8, cudaMemcpyHostToDevice));
-  CUDA_TRY(cudaMemcpy(st.tree_ids, v->tree_ids, S * 2, cudaMemcpyHostToDevice));
-  CUDA_TRY(cudaMemcpy(st.active, v->active_counts, S * 4, cudaMemcpyHostToDevice));
-  CUDA_TRY(cudaMemcpy(st.qc, v->queue_counters, S * 4, cudaMemcpyHostToDevice));
-  CUDA_TRY(cudaMemcpy(st.qfc, v->queue_free_counters, S * 4, cudaMemcpyHostToDevice));
-  CUDA_TRY(cudaMemcpy(st.fqfc, v->final_queue_free_counters, S * 4, cudaMemcpyHostToDevice));
-  CUDA_TRY(cudaMemcpy(st.fctr, v->free_counters, nb * 4, cudaMemcpyHostToDevice));
-  CUDA_TRY(cudaMemcpy(st.queues, v->queues, nb * 4, cudaMemcpyHostToDevice));
-  CUDA_TRY(cudaMemcpy(st.slots, v->slots, (uint64_t)st.total_slots * 4, cudaMemcpyHostToDevice));
+  const cudaMemcpyKind H2D = cudaMemcpyHostToDevice;
+  CUDA_TRY(cudaMemcpy(st.seg_tree, v->seg_tree_words, W * 8, H2D));
+  CUDA_TRY(cudaMemcpy(st.sub_trees, v->sub_tree_words, T * W * 8, H2D));
+  CUDA_TRY(cudaMemcpy(st.tree_ids, v->tree_ids, S * 2, H2D));
+  {
+    std::vector<unsigned long long> act(S);  // generation 0, the view's counts
+    for (uint64_t i = 0; i < S; i++) act[i] = gal::act_word(0, v->active_counts[i]);
+    CUDA_TRY(cudaMemcpy(st.act, act.data(), S * 8, H2D));
+  }
+  CUDA_TRY(cudaMemcpy(st.qc, v->queue_counters, S * 4, H2D));
+  CUDA_TRY(cudaMemcpy(st.qfc, v->queue_free_counters, S * 4, H2D));
+  CUDA_TRY(cudaMemcpy(st.fqfc, v->final_queue_free_counters, S * 4, H2D));
+  CUDA_TRY(cudaMemcpy2D(st.fctr, (size_t)st.fstride * 4, v->free_counters, 4, 4, nb, H2D));
+  CUDA_TRY(cudaMemcpy(st.queues, v->queues, nb * 4, H2D));
+  CUDA_TRY(cudaMemcpy(st.slots, v->slots, (uint64_t)st.total_slots * 4, H2D));
   CUDA_TRY(cudaMemset(st.spares, 0xFF, (uint64_t)st.total_slots * 4));  // the view holds none
   uint32_t *d_mc = nullptr;
   CUDA_TRY(cudaMalloc(&d_mc, nb * 4));
-  cudaError_t e = cudaMemcpy(d_mc, v->malloc_counters, nb * 4, cudaMemcpyHostToDevice);
+  cudaError_t e = cudaMemcpy(d_mc, v->malloc_counters, nb * 4, H2D);
   if (e == cudaSuccess) {
     k_import_blocks<<<1024, 256>>>(h->d_state, d_mc, nb);
     e = cudaDeviceSynchronize();
   }
   cudaFree(d_mc);
   if (e != cudaSuccess) return GAL_ERR_CUDA;
-  uint32_t locks = v->locks;
-  CUDA_TRY(cudaMemcpy(st.locks, &locks, 4, cudaMemcpyHostToDevice));
+  uint32_t locks[GAL_MAX_TREES + 1];
+  for (uint32_t t = 0; t <= T; t++) locks[t] = (v->locks >> t) & 1u;
+  CUDA_TRY(cudaMemcpy2D(st.locks, gal::LOCK_STRIDE * 4, locks, 4, 4, T + 1, H2D));
   return GAL_OK;
 }
 
@@ -835,3 +858,6 @@ int gal_free_batched_n(gal_handle *h, void *const *ptrs, const unsigned long lon
 }
 
 }  // extern "C"
+
+int gal_internal_device(const gal_handle *h) { return h->device; }
+const gal::state *gal_internal_host_state(const gal_handle *h) { return &h->st; }

@@ -1,33 +1,41 @@
 // gal_noalloc.cu — state export that allocates no device memory.
 //
 // gal_export_state() stages the per-block malloc counters through a device
-// buffer it gets from cudaMalloc and gives back with cudaFree.  Some callers
-// cannot do that: a framework whose caching allocator has already reserved the
-// device's memory (a fresh cudaMalloc can fail even though the allocator's own
-// state is readable), a monitor that snapshots the allocator while other
-// streams keep running (cudaFree waits for the whole device), or code with a
-// fixed device-memory budget.  gal_export_state_noalloc() does the same export
-// with its staging area in a fixed array that is part of this library's
-// device image.
+// buffer it gets from cudaMalloc and gives back with cudaFree, and waits for
+// the whole device first.  Some callers cannot do either: a framework whose
+// caching allocator has already reserved the device's memory (a fresh
+// cudaMalloc can fail even though the allocator's own state is readable), a
+// monitor that snapshots the allocator while other streams keep running
+// (cudaFree and cudaDeviceSynchronize wait for all of them), or code with a
+// fixed device-memory budget.  gal_export_state_noalloc() does the same
+// export with its staging area in a fixed array that is part of this
+// library's device image, on a stream of its own, and waits for that stream
+// only.
 //
 // Limits and sharing:
 //   * the array holds GAL_NOALLOC_MAX_BLOCKS block counters (1 MiB); larger
 //     allocators are rejected with GAL_ERR_ARGS and a message;
 //   * every GPU that loads the library keeps this 1 MiB until the process exits;
-//   * the first call on a device looks up the array's device address (with
-//     that device current) and caches it; make that first call before any
-//     stream capture;
+//   * set-up, once per device with that device current: the array's device
+//     address is looked up (which loads this file's module, placing the array
+//     on the device) and the export's stream is created.  gal_create does it
+//     for the device it builds on, so the export itself allocates nothing; a
+//     handle's first export on a device that was never set up does it then,
+//     and that call should come before any stream capture;
 //   * all calls share the one array and it keeps the last call's contents;
 //     each call writes every entry it reads back, so nothing needs clearing,
 //     but calls that overlap on the GPU (for example from two host threads at
-//     once) race on it.
+//     once) race on it;
+//   * the copies run while other streams may still be changing the state, so
+//     a snapshot taken during device malloc/free is not a consistent cut: each
+//     word holds some value it had during the call.  With no device work on
+//     the allocator in flight it equals gal_export_state's result.
 #include <cuda_runtime.h>
 #include <stdio.h>
 
 #include <mutex>
 
-#include "../../include/gallatin_gb300.h"
-#include "../../include/gallatin_gb300/gal_device.cuh"
+#include "gal_internal.h"
 
 namespace {
 
@@ -36,25 +44,25 @@ constexpr uint64_t kMaxBlocks = GAL_NOALLOC_MAX_BLOCKS;
 static __device__ __align__(256) uint32_t g_export_scratch[kMaxBlocks];
 
 constexpr int kMaxDevices = 64;
+struct per_device {
+  uint32_t *scratch = nullptr;   // device address of g_export_scratch
+  cudaStream_t stream = nullptr; // the export's own non-blocking stream
+};
 std::mutex g_mu;
-uint32_t *g_scratch_addr[kMaxDevices] = {};
+per_device g_dev[kMaxDevices];
 
 // per-block malloc counters in the reference packing, written into `out`
 __global__ void k_export_blocks_fixed(const gal::state *s, uint32_t *out, uint64_t nblocks) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t b = i; b < nblocks; b += stride) {
-    unsigned long long w = s->mwords[b];
-    out[b] = (uint32_t)(((w >> 32) << 20) + (w & 0xFFFFFFFFull));
-  }
+  for (uint64_t b = i; b < nblocks; b += stride) out[b] = gal::export_mword(s, (uint32_t)b);
 }
 
-// device address of the scratch array on the current device (looked up once)
-int scratch_for_current_device(uint32_t **out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return GAL_ERR_CUDA;
-  std::lock_guard<std::mutex> g(g_mu);
-  if (!g_scratch_addr[dev]) {
+// set-up for `dev`, which must be current; the caller holds g_mu
+int setup_locked(int dev) {
+  if (dev < 0 || dev >= kMaxDevices) return GAL_ERR_CUDA;
+  per_device &d = g_dev[dev];
+  if (!d.scratch) {
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_export_scratch);
     if (e != cudaSuccess || !p) {
@@ -62,9 +70,16 @@ int scratch_for_current_device(uint32_t **out) {
               cudaGetErrorString(e));
       return GAL_ERR_CUDA;
     }
-    g_scratch_addr[dev] = (uint32_t *)p;
+    d.scratch = (uint32_t *)p;
   }
-  *out = g_scratch_addr[dev];
+  if (!d.stream) {
+    cudaError_t e = cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      fprintf(stderr, "gallatin_gb300: creating the export stream failed: %s\n", cudaGetErrorString(e));
+      d.stream = nullptr;
+      return GAL_ERR_CUDA;
+    }
+  }
   return GAL_OK;
 }
 
@@ -79,11 +94,15 @@ int scratch_for_current_device(uint32_t **out) {
 
 }  // namespace
 
-extern "C" int gal_export_state_noalloc(gal_handle *h, const gal_state_view *v) {
+int gal_noalloc_setup(int device) {
+  std::lock_guard<std::mutex> g(g_mu);
+  return setup_locked(device);
+}
+
+extern "C" int gal_export_state_noalloc(gal_handle *h, gal_state_view *v) {
   if (!h || !v) return GAL_ERR_ARGS;
-  gal_state_dims d;
-  if (gal_state_dims_get(h, &d) != GAL_OK) return GAL_ERR_ARGS;
-  const uint64_t S = d.num_segments, nb = S * d.blocks_per_segment, W = d.veb_words, T = d.num_trees;
+  const gal::state &st = *gal_internal_host_state(h);
+  const uint64_t S = st.num_segments, nb = S << st.bps_shift, W = st.veb.words, T = st.num_trees;
   if (nb > kMaxBlocks) {
     fprintf(stderr,
             "gallatin_gb300: gal_export_state_noalloc handles at most %llu blocks "
@@ -91,30 +110,41 @@ extern "C" int gal_export_state_noalloc(gal_handle *h, const gal_state_view *v) 
             (unsigned long long)kMaxBlocks, (unsigned long long)nb);
     return GAL_ERR_ARGS;
   }
-  uint32_t *scratch = nullptr;
-  int rc = scratch_for_current_device(&scratch);
-  if (rc != GAL_OK) return rc;
+  const int dev = gal_internal_device(h);
+  gal_device_guard on_dev(dev);  // the handle's device, whatever the caller's current one
+  TRY(on_dev.err);
+  per_device d;
+  {
+    std::lock_guard<std::mutex> g(g_mu);
+    int rc = setup_locked(dev);
+    if (rc != GAL_OK) return rc;
+    d = g_dev[dev];
+  }
   const gal::state *d_state = (const gal::state *)gal_device_state(h);
-  gal::state st;  // host copy of the device-resident state: array addresses
-  TRY(cudaDeviceSynchronize());
-  TRY(cudaMemcpy(&st, d_state, sizeof(st), cudaMemcpyDeviceToHost));
-  TRY(cudaMemcpy(v->seg_tree_words, st.seg_tree, W * 8, cudaMemcpyDeviceToHost));
-  TRY(cudaMemcpy(v->sub_tree_words, st.sub_trees, T * W * 8, cudaMemcpyDeviceToHost));
-  TRY(cudaMemcpy(v->tree_ids, st.tree_ids, S * 2, cudaMemcpyDeviceToHost));
-  TRY(cudaMemcpy(v->active_counts, st.active, S * 4, cudaMemcpyDeviceToHost));
-  TRY(cudaMemcpy(v->queue_counters, st.qc, S * 4, cudaMemcpyDeviceToHost));
-  TRY(cudaMemcpy(v->queue_free_counters, st.qfc, S * 4, cudaMemcpyDeviceToHost));
-  TRY(cudaMemcpy(v->final_queue_free_counters, st.fqfc, S * 4, cudaMemcpyDeviceToHost));
-  TRY(cudaMemcpy(v->free_counters, st.fctr, nb * 4, cudaMemcpyDeviceToHost));
-  TRY(cudaMemcpy(v->queues, st.queues, nb * 4, cudaMemcpyDeviceToHost));
-  TRY(cudaMemcpy(v->slots, st.slots, (uint64_t)st.total_slots * 4, cudaMemcpyDeviceToHost));
-  k_export_blocks_fixed<<<1024, 256>>>(d_state, scratch, nb);
+  cudaStream_t s = d.stream;
+  const cudaMemcpyKind D2H = cudaMemcpyDeviceToHost;
+  TRY(cudaMemcpyAsync(v->seg_tree_words, st.seg_tree, W * 8, D2H, s));
+  TRY(cudaMemcpyAsync(v->sub_tree_words, st.sub_trees, T * W * 8, D2H, s));
+  TRY(cudaMemcpyAsync(v->tree_ids, st.tree_ids, S * 2, D2H, s));
+  // the low half of each segment's count word (its biased count), then unbiased below
+  TRY(cudaMemcpy2DAsync(v->active_counts, 4, st.act, 8, 4, S, D2H, s));
+  TRY(cudaMemcpyAsync(v->queue_counters, st.qc, S * 4, D2H, s));
+  TRY(cudaMemcpyAsync(v->queue_free_counters, st.qfc, S * 4, D2H, s));
+  TRY(cudaMemcpyAsync(v->final_queue_free_counters, st.fqfc, S * 4, D2H, s));
+  TRY(cudaMemcpy2DAsync(v->free_counters, 4, st.fctr, (size_t)st.fstride * 4, 4, nb, D2H, s));
+  TRY(cudaMemcpyAsync(v->queues, st.queues, nb * 4, D2H, s));
+  TRY(cudaMemcpyAsync(v->slots, st.slots, (uint64_t)st.total_slots * 4, D2H, s));
+  k_export_blocks_fixed<<<1024, 256, 0, s>>>(d_state, d.scratch, nb);
   TRY(cudaGetLastError());
-  TRY(cudaMemcpy(v->malloc_counters, scratch, nb * 4, cudaMemcpyDeviceToHost));
-  uint32_t locks = 0, err = 0;
-  TRY(cudaMemcpy(&locks, st.locks, 4, cudaMemcpyDeviceToHost));
-  TRY(cudaMemcpy(&err, st.error, 4, cudaMemcpyDeviceToHost));
-  ((gal_state_view *)v)->locks = locks;
-  ((gal_state_view *)v)->error_word = err;
+  TRY(cudaMemcpyAsync(v->malloc_counters, d.scratch, nb * 4, D2H, s));
+  uint32_t locks[GAL_MAX_TREES + 1] = {}, err = 0;
+  TRY(cudaMemcpy2DAsync(locks, 4, st.locks, gal::LOCK_STRIDE * 4, 4, T + 1, D2H, s));
+  TRY(cudaMemcpyAsync(&err, st.error, 4, D2H, s));
+  TRY(cudaStreamSynchronize(s));
+  for (uint64_t i = 0; i < S; i++) v->active_counts[i] = gal::act_unbias((uint32_t)v->active_counts[i]);
+  uint32_t bits = 0;
+  for (uint32_t t = 0; t <= T; t++) bits |= locks[t] ? 1u << t : 0u;
+  v->locks = bits;
+  v->error_word = err;
   return GAL_OK;
 }

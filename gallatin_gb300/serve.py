@@ -4,16 +4,20 @@ Jobs arrive as a Poisson process (default mean 2,000 jobs/s, seed 5).  A job is
 either a device vector of uint32 grown by push_back to n elements (n
 log-uniform over 1K-16M, capacity doubling through the allocator) or a queue
 of 32 B nodes with n enqueue/dequeue operations (n log-uniform over 1K-4M);
-each runs as one CTA (gal_job_launch) on a stream slot.  The loop keeps every
+each runs as a grid of up to 8 CTAs (gal_job_launch, gal_job_ctas) on a stream
+slot.  The loop keeps every
 slot busy: a job that has arrived is admitted as soon as a slot is free and the
 arena bytes reserved by running jobs plus its own estimated footprint fit in
 the budget, so jobs arriving while others run overlap with them on the device.
 Allocator state stays resident on the device across all jobs.
 
-Reported: malloc+free ops/s over the whole run, job latency (completion -
-arrival) p50/p99, per-request malloc/free latency p50/p99 in SM cycles
-(clock64 around the first calls of each job), failures.  `solo_check` reruns
-jobs one at a time and compares their checksums with the mixed run.
+Reported: malloc+free ops/s over the whole run; job latency (host-observed
+completion - arrival) p50/p99, split into the admission wait (admission -
+arrival, the host loop) and the job's device time (CUDA events around its
+launch on its stream); per-request malloc/free latency p50/p99 in SM cycles
+over every malloc and free of every job (clock64 around each call, counted in
+a device histogram of four bins per power of two); failures.  `solo_check`
+reruns jobs one at a time and compares their checksums with the mixed run.
 """
 import ctypes as C
 import time
@@ -24,8 +28,44 @@ import numpy as np
 from . import GAL_OK, Gallatin, GalError, lib
 
 JOB_VECTOR, JOB_QUEUE = 0, 1
-LAT = 64
+LAT_BINS = 160   # GAL_JOB_LAT_BINS
 SEG = 16 << 20
+
+
+def job_ctas(kind, n):
+    """CTAs of a job (gal_job_ctas): one per 2^20 vector elements or 2^18
+    queue operations, 1 to 8."""
+    g = n >> 20 if kind == JOB_VECTOR else n >> 18
+    return int(min(8, max(1, g)))
+
+
+def lat_bin(c):
+    """Histogram bin of c cycles, as gal_job_launch bins them."""
+    if c < 4:
+        return int(c)
+    e = int(c).bit_length() - 1
+    return min(4 * e + ((int(c) >> (e - 2)) & 3), LAT_BINS - 1)
+
+
+def bin_value(b):
+    """Cycles a latency bin stands for (the middle of its range; gal_job_launch
+    puts c cycles in bin c below 4, else in 4 floor(log2 c) + the two bits
+    below the leading one)."""
+    if b < 4:
+        return float(b)
+    e, m = b // 4, b % 4
+    lo = (1 << e) + m * (1 << (e - 2))
+    return lo + ((1 << (e - 2)) - 1) / 2.0
+
+
+def hist_percentile(counts, q):
+    """q-th percentile (0-100) of a latency histogram, as its bin's value."""
+    counts = np.asarray(counts, dtype=np.float64)
+    total = counts.sum()
+    if total == 0:
+        return None
+    b = int(np.searchsorted(np.cumsum(counts), q / 100.0 * total, side="left"))
+    return bin_value(min(b, len(counts) - 1))
 
 
 def make_jobs(num_jobs, rate=2000.0, seed=5, vector_share=0.5):
@@ -41,10 +81,12 @@ def make_jobs(num_jobs, rate=2000.0, seed=5, vector_share=0.5):
 def footprint(kind, n):
     """Peak arena bytes a job can hold (admission estimate)."""
     if kind == JOB_VECTOR:
-        cap = max(1024, 1 << int(np.ceil(np.log2(max(n, 1)))))
-        new, old = 4 * cap, 2 * cap              # bytes of the last two buffers
+        g = job_ctas(kind, n)
+        share = -(-n // g)                        # elements of the largest CTA share
+        cap = max(1024, 1 << int(np.ceil(np.log2(max(share, 1)))))
+        new, old = 4 * cap, 2 * cap              # bytes of the last two buffers of a CTA
         r = lambda b: ((b - 1) // SEG + 1) * SEG if b > SEG else 1 << int(np.ceil(np.log2(b)))
-        return r(new) + r(old)
+        return g * (r(new) + r(old))
     return 32 * n + SEG                           # every operation an enqueue, at most
 
 
@@ -106,10 +148,10 @@ class Server:
         self.streams = [torch.cuda.Stream() for _ in range(slots)]
         self.budget = budget_bytes if budget_bytes is not None else int(0.85 * g.arena_bytes)
 
-    def _launch(self, job, row, results, lats, stream):
+    def _launch(self, job, row, results, hist, stream):
         rc = lib().gal_job_launch(self.g.handle, job["kind"], job["id"], job["n"],
                                   C.c_void_p(results[row].data_ptr()),
-                                  C.c_void_p(lats[row].data_ptr()), C.c_void_p(stream.cuda_stream))
+                                  C.c_void_p(hist.data_ptr()), C.c_void_p(stream.cuda_stream))
         if rc != GAL_OK:
             raise GalError(f"gal_job_launch failed ({rc})")
 
@@ -117,16 +159,19 @@ class Server:
         torch = self.torch
         nj = len(jobs)
         results = torch.zeros((nj, 3), dtype=torch.int64, device="cuda")
-        lats = torch.zeros((nj, 2 * LAT), dtype=torch.int32, device="cuda")
+        hist = torch.zeros(2 * LAT_BINS, dtype=torch.int64, device="cuda")
         torch.cuda.synchronize()
         jobs = [dict(j, row=r) for r, j in enumerate(jobs)]  # result rows follow the input order
+        events = [None] * nj
 
         def launch(job, slot):
             s = self.streams[slot]
-            self._launch(job, job["row"], results, lats, s)
-            ev = torch.cuda.Event()
-            ev.record(s)
-            return ev
+            start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            start.record(s)
+            self._launch(job, job["row"], results, hist, s)
+            end.record(s)
+            events[job["row"]] = (start, end)
+            return end
 
         t0 = time.perf_counter()
         admit_t, done_t, max_running = schedule(jobs, self.slots, self.budget, launch,
@@ -134,21 +179,27 @@ class Server:
         wall = time.perf_counter() - t0
         torch.cuda.synchronize()
         res = results.cpu().numpy()
-        lat = lats.cpu().numpy().astype(np.uint32)
+        h = hist.cpu().numpy()
+        mh, fh = h[:LAT_BINS], h[LAT_BINS:]
         arrival = np.array([j["arrival"] for j in jobs])
         job_lat = done_t - (arrival if realtime else admit_t)
-        m_cyc = lat[:, :LAT][lat[:, :LAT] > 0]
-        f_cyc = lat[:, LAT:][lat[:, LAT:] > 0]
+        wait = admit_t - arrival if realtime else np.zeros(nj)
+        dev_ms = np.array([a.elapsed_time(b) for a, b in events])
         ops = int(res[:, 1].sum())
         return {
             "jobs": nj, "ops": ops, "wall_s": wall, "ops_per_s": ops / wall,
             "failed_mallocs": int(res[:, 2].sum()), "max_concurrent_jobs": max_running,
             "job_latency_ms_p50": float(np.percentile(job_lat, 50) * 1e3),
             "job_latency_ms_p99": float(np.percentile(job_lat, 99) * 1e3),
-            "malloc_cycles_p50": float(np.percentile(m_cyc, 50)) if len(m_cyc) else None,
-            "malloc_cycles_p99": float(np.percentile(m_cyc, 99)) if len(m_cyc) else None,
-            "free_cycles_p50": float(np.percentile(f_cyc, 50)) if len(f_cyc) else None,
-            "free_cycles_p99": float(np.percentile(f_cyc, 99)) if len(f_cyc) else None,
+            "admission_wait_ms_p50": float(np.percentile(wait, 50) * 1e3),
+            "admission_wait_ms_p99": float(np.percentile(wait, 99) * 1e3),
+            "job_device_ms_p50": float(np.percentile(dev_ms, 50)),
+            "job_device_ms_p99": float(np.percentile(dev_ms, 99)),
+            "latency_requests": {"mallocs": int(mh.sum()), "frees": int(fh.sum())},
+            "malloc_cycles_p50": hist_percentile(mh, 50),
+            "malloc_cycles_p99": hist_percentile(mh, 99),
+            "free_cycles_p50": hist_percentile(fh, 50),
+            "free_cycles_p99": hist_percentile(fh, 99),
             "checksums": res[:, 0].astype(np.uint64), "error_word": self.g.error_word(),
         }
 

@@ -56,35 +56,80 @@ def check_live(ptrs, sizes, base):
     return overlap, misaligned
 
 
+class TorchBackend:
+    """large_block_workload's view of this library's allocator: per-thread
+    malloc/free calls through the C ABI on device arrays, timed with CUDA
+    events around each launch."""
+
+    def __init__(self, g):
+        import torch
+        self.g = g
+        self.arena_bytes = g.arena_bytes
+        self.arena_base = g.arena_base
+        self._ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+
+    def _timed(self, fn, *args):
+        ev0, ev1 = self._ev
+        ev0.record()
+        fn(*args)
+        ev1.record()
+        ev1.synchronize()
+        return ev0.elapsed_time(ev1)
+
+    def malloc(self, sizes):
+        import torch
+        d_sizes = torch.from_numpy(np.ascontiguousarray(sizes, dtype=np.int64)).cuda()
+        d_ptrs = torch.zeros(len(sizes), dtype=torch.int64, device="cuda")
+        ms = self._timed(self.g.malloc_per_thread, d_sizes, d_ptrs)
+        return d_ptrs.cpu().numpy(), ms
+
+    def free(self, ptrs):
+        import torch
+        d_ptrs = torch.from_numpy(np.ascontiguousarray(ptrs, dtype=np.int64)).cuda()
+        return self._timed(self.g.free_per_thread, d_ptrs)
+
+    def free_runs(self):
+        """(largest run of free segments, free segments)"""
+        st = self.g.stats()
+        return int(st.largest_free_run), int(st.free_segments)
+
+    def extra(self):
+        st = self.g.stats()
+        return {"multi_segment_allocs_after_drain": int(st.multi_segment_allocs),
+                "error_word": self.g.error_word()}
+
+
+def largest_run_of_ones(words, n):
+    """Longest run of set bits among the first n bits of a u64 word array."""
+    bits = np.unpackbits(np.ascontiguousarray(words, dtype="<u8").view(np.uint8), bitorder="little")[:n]
+    if not bits.any():
+        return 0
+    edges = np.diff(np.concatenate([[0], bits.astype(np.int8), [0]]))
+    return int((np.flatnonzero(edges == -1) - np.flatnonzero(edges == 1)).max())
+
+
 def large_block_workload(g, seed=3, fill=0.70, rounds=10, small_per_large=20, batch=256,
                          free_frac=0.30):
-    import torch
-
+    """Runs the workload on `g`: a Gallatin (this library) or any backend with
+    malloc(sizes) -> (pointers, ms), free(pointers) -> ms, free_runs(),
+    extra(), arena_bytes and arena_base."""
+    be = g if hasattr(g, "free_runs") else TorchBackend(g)
     rng = np.random.default_rng(seed)
-    arena = g.arena_bytes
+    arena = be.arena_bytes
     target = fill * arena
     live_p = np.zeros(0, dtype=np.int64)
     live_s = np.zeros(0, dtype=np.int64)
     stats = {"mallocs": 0, "frees": 0, "failed": 0, "large_requests": 0, "gpu_ms": 0.0,
              "fragmentation": [], "overlaps": 0, "misaligned": 0}
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-
-    def timed(fn, *args):
-        ev0.record()
-        fn(*args)
-        ev1.record()
-        ev1.synchronize()
-        stats["gpu_ms"] += ev0.elapsed_time(ev1)
 
     def allocate(n_large):
         nonlocal live_p, live_s
         large = (2 ** rng.uniform(16, 28, n_large)).astype(np.int64)
         sizes = np.concatenate([large, np.full(n_large * small_per_large, 64, dtype=np.int64)])
         rng.shuffle(sizes)
-        d_sizes = torch.from_numpy(sizes).cuda()
-        d_ptrs = torch.zeros(len(sizes), dtype=torch.int64, device="cuda")
-        timed(g.malloc_per_thread, d_sizes, d_ptrs)
-        ptrs = d_ptrs.cpu().numpy()
+        ptrs, ms = be.malloc(sizes)
+        ptrs = np.asarray(ptrs).view(np.int64)
+        stats["gpu_ms"] += ms
         ok = ptrs != 0
         stats["mallocs"] += int(ok.sum())
         stats["failed"] += int((~ok).sum())
@@ -99,30 +144,26 @@ def large_block_workload(g, seed=3, fill=0.70, rounds=10, small_per_large=20, ba
                 break
 
     def round_report():
-        o, m = check_live(live_p, live_s, g.arena_base)
+        o, m = check_live(live_p, live_s, be.arena_base)
         stats["overlaps"] += o
         stats["misaligned"] += m
-        st = g.stats()
-        frag = st.largest_free_run / st.free_segments if st.free_segments else 1.0
+        run, free = be.free_runs()
+        frag = run / free if free else 1.0
         stats["fragmentation"].append(round(float(frag), 4))
 
     fill_up()
     round_report()
     for _ in range(rounds):
         victims = rng.random(len(live_p)) < free_frac
-        d_free = torch.from_numpy(live_p[victims]).cuda()
-        timed(g.free_per_thread, d_free)
+        stats["gpu_ms"] += be.free(live_p[victims])
         stats["frees"] += int(victims.sum())
         live_p, live_s = live_p[~victims], live_s[~victims]
         fill_up()
         round_report()
     # drain
-    d_free = torch.from_numpy(live_p).cuda()
-    timed(g.free_per_thread, d_free)
+    stats["gpu_ms"] += be.free(live_p)
     stats["frees"] += len(live_p)
-    st = g.stats()
-    stats["multi_segment_allocs_after_drain"] = int(st.multi_segment_allocs)
-    stats["error_word"] = g.error_word()
+    stats.update(be.extra())
     stats["ops_per_s"] = (stats["mallocs"] + stats["frees"]) / (stats["gpu_ms"] / 1e3)
     stats["live_fraction_target"] = fill
     return stats

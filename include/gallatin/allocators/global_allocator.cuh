@@ -14,6 +14,11 @@
 // call init_global_allocator in the translation unit whose kernels use
 // global_malloc/global_free.  The instance itself is the process-global one
 // of the C ABI (gal_init / gal_teardown).
+//
+// A handle that was never set in this translation unit, or was cleared by
+// free_global_allocator, is null: global_malloc then returns nullptr (the
+// reference's failure value, global_allocator.cuh:72-76) and global_free does
+// nothing, instead of dereferencing the null handle.
 #pragma once
 
 #include "gallatin.cuh"
@@ -56,9 +61,15 @@ __host__ inline void free_global_allocator() {
   cudaMemcpyToSymbol(global_gallatin, &null_copy, sizeof(global_allocator_type *));
 }
 
-__device__ __forceinline__ void *global_malloc(uint64_t num_bytes) { return global_gallatin->malloc(num_bytes); }
+__device__ __forceinline__ void *global_malloc(uint64_t num_bytes) {
+  global_allocator_type *a = global_gallatin;
+  return a ? a->malloc(num_bytes) : nullptr;
+}
 
-__device__ __forceinline__ void global_free(void *ptr) { global_gallatin->free(ptr); }
+__device__ __forceinline__ void global_free(void *ptr) {
+  global_allocator_type *a = global_gallatin;
+  if (a) a->free(ptr);
+}
 
 __host__ inline void print_global_stats() {
   gal_handle *h = gal_global();
@@ -94,10 +105,14 @@ __host__ inline void free_global_allocator_host() {
 }
 
 __device__ __forceinline__ void *global_malloc_host(uint64_t num_bytes) {
-  return global_host_gallatin->malloc(num_bytes);
+  global_allocator_type *a = global_host_gallatin;
+  return a ? a->malloc(num_bytes) : nullptr;
 }
 
-__device__ __forceinline__ void global_free_host(void *ptr) { global_host_gallatin->free(ptr); }
+__device__ __forceinline__ void global_free_host(void *ptr) {
+  global_allocator_type *a = global_host_gallatin;
+  if (a) a->free(ptr);
+}
 
 __host__ inline void print_global_stats_host() {
   gal_handle *h = gal_global_host();
@@ -134,7 +149,8 @@ __device__ __forceinline__ void *global_malloc_fused(uint64_t num_bytes) {
 }
 
 __device__ __forceinline__ void global_free_fused(void *ptr) {
-  if (global_gallatin->owns_allocation(ptr)) global_free(ptr);
+  global_allocator_type *a = global_gallatin;
+  if (a && a->owns_allocation(ptr)) global_free(ptr);
   else global_free_host(ptr);
 }
 
@@ -150,9 +166,11 @@ __host__ inline void print_global_stats_combined() {
 // the region holds 0, 1, 2, ... and the 16 bytes after it repeat the record.
 
 __device__ inline void *global_malloc_poison(uint64_t bytes_needed) {
-  const uint64_t total = global_gallatin->get_allocated_size(bytes_needed + 32);
+  global_allocator_type *a = global_gallatin;
+  if (!a) return nullptr;
+  const uint64_t total = a->get_allocated_size(bytes_needed + 32);
   const uint64_t extra = total - (bytes_needed + 32);
-  char *base = (char *)global_gallatin->malloc(bytes_needed + 32);
+  char *base = (char *)a->malloc(bytes_needed + 32);
   if (!base) return nullptr;
   uint64_t *head = (uint64_t *)base;
   uint64_t *tail = (uint64_t *)(base + 16 + bytes_needed + extra);

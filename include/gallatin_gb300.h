@@ -95,7 +95,21 @@ typedef struct gal_config {
                                    clearing them in child kernels (dynamic
                                    parallelism); here the allocating thread
                                    clears its own bytes.  Default 0.            */
+  uint32_t block_layout;        /* GAL_BLOCK_LAYOUT_*: where each block's malloc
+                                   and free counters live.  RECORD (default):
+                                   both in one 32-byte record, one L2 sector per
+                                   block, so the blocks that different SMs claim
+                                   from at the same time never share a sector.
+                                   DENSE: all malloc words in one array (8 B
+                                   each), all free counters in another (4 B).
+                                   The reference's Block is the dense 8-byte
+                                   pair (block.cuh:59); offsets are the same
+                                   either way.                                   */
 } gal_config;
+
+/* Block counter layouts (gal_config.block_layout). */
+#define GAL_BLOCK_LAYOUT_DENSE 0u
+#define GAL_BLOCK_LAYOUT_RECORD 1u
 
 /* Arena backing (gal_config.arena_kind). */
 #define GAL_ARENA_DEVICE 0u  /* cudaMalloc (generate_on_device, gallatin.cuh:324)  */
@@ -198,20 +212,26 @@ int gal_error_info(gal_handle *h, uint64_t *out4);
 /* State view export/import (no reference counterpart: a snapshot of every
  * metadata array, for parity tests and drain checks). */
 int gal_state_dims_get(gal_handle *h, gal_state_dims *out);
-int gal_export_state(gal_handle *h, const gal_state_view *view);
+int gal_export_state(gal_handle *h, gal_state_view *view);
 int gal_import_state(gal_handle *h, const gal_state_view *view);
 
-/* Same result as gal_export_state, without allocating device memory: for
- * callers that cannot cudaMalloc/cudaFree at this point (a caching allocator
- * already holds the device's memory, the snapshot must not wait for the whole
- * device, or the device-memory budget is fixed).  No counterpart in the
+/* Same result as gal_export_state, without allocating device memory and
+ * without waiting for the whole device: for callers that cannot
+ * cudaMalloc/cudaFree at this point (a caching allocator already holds the
+ * device's memory, or the device-memory budget is fixed) and for monitors
+ * that snapshot while other streams keep running.  No counterpart in the
  * reference.  Stages the block counters in a fixed 1 MiB device array
  * (GAL_NOALLOC_MAX_BLOCKS counters) that every GPU loading the library keeps
- * until exit; larger allocators get GAL_ERR_ARGS.  The first call on a device
- * looks the array up and should come before any stream capture; calls share
- * the array, so calls that overlap on the GPU race. */
+ * until exit; larger allocators get GAL_ERR_ARGS.  Runs on a stream of its
+ * own and waits for that stream only, on the handle's device.  gal_create
+ * sets the array and the stream up on its device, so the call itself loads
+ * and allocates nothing; a first call on a device that was never set up does
+ * the set-up then and should come before any stream capture.  Calls share the
+ * array, so calls that overlap on the GPU race.  While device malloc/free run
+ * on other streams the copy is not a consistent cut (each word holds some
+ * value it had during the call). */
 #define GAL_NOALLOC_MAX_BLOCKS (1u << 18)
-int gal_export_state_noalloc(gal_handle *h, const gal_state_view *view);
+int gal_export_state_noalloc(gal_handle *h, gal_state_view *view);
 
 /* Change the pinned-slot smid override after creation (-1 = hardware). */
 int gal_set_smid_override(gal_handle *h, int32_t smid);
@@ -291,18 +311,24 @@ int gal_free_batched_n(gal_handle *h, void *const *ptrs, const unsigned long lon
                        uint64_t max_n, void *stream);
 
 /* ---- served jobs (request loop, gallatin_gb300/serve.py) -------------------
- * One job = one CTA launched on `stream` that allocates through the device
- * allocator: GAL_JOB_VECTOR grows a device vector of n uint32 by capacity
- * doubling (the reference's data_structs/single_vector.cuh:86-143 growth);
- * GAL_JOB_QUEUE runs n enqueue/dequeue operations on queues of 32 B nodes.
- * result (device u64[3], zeroed by the caller): checksum, mallocs+frees,
- * failed mallocs.  lat (device u32[2*GAL_JOB_LAT_SAMPLES] or NULL): cycles of
- * the first mallocs, then of the first frees, of the job's first thread. */
+ * One job = a grid of gal_job_ctas(kind, n) CTAs launched on `stream` that
+ * allocate through the device allocator: GAL_JOB_VECTOR grows device vectors
+ * of uint32 by capacity doubling (the reference's
+ * data_structs/single_vector.cuh:86-143 growth), CTA b of G over elements
+ * [b n / G, (b + 1) n / G); GAL_JOB_QUEUE runs n enqueue/dequeue operations
+ * on queues of 32 B nodes.  result (device u64[3], zeroed by the caller):
+ * checksum, mallocs+frees, failed mallocs.  hist (device
+ * u64[2 * GAL_JOB_LAT_BINS] or NULL): the job adds the latency of each of its
+ * mallocs (bins 0..GAL_JOB_LAT_BINS-1) and frees (the next GAL_JOB_LAT_BINS),
+ * in SM cycles measured with clock64 around the call; c cycles fall in bin c
+ * for c < 4, else in bin 4 floor(log2 c) + ((c >> (floor(log2 c) - 2)) & 3),
+ * the last bin taking everything above. */
 #define GAL_JOB_VECTOR 0u
 #define GAL_JOB_QUEUE 1u
-#define GAL_JOB_LAT_SAMPLES 64
+#define GAL_JOB_LAT_BINS 160
+uint32_t gal_job_ctas(uint32_t kind, uint64_t n);
 int gal_job_launch(gal_handle *h, uint32_t kind, uint64_t job_id, uint64_t n,
-                   unsigned long long *result, uint32_t *lat, void *stream);
+                   unsigned long long *result, unsigned long long *hist, void *stream);
 
 #ifdef __cplusplus
 }

@@ -14,7 +14,14 @@
 //   * the malloc word of a block is 64-bit: (tree << 32) | count, so stale
 //     claims can never carry a count into the tree field (the reference packs
 //     tree << 20 | count into 32 bits, block.cuh:53);
-//   * malloc and free counters live in separate arrays (different L2 lines);
+//   * a block's malloc and free counters share one 32-byte record (one L2
+//     sector per block, gal_config.block_layout), so the pinned blocks that
+//     different SMs claim from never share a sector; the dense layout (all
+//     malloc words, then all free counters) remains selectable;
+//   * each segment's count of blocks left carries a set-up generation, so a
+//     reservation checks the segment's class before it subtracts and never
+//     has to give back into a later owner's count;
+//   * every class lock sits in a 32-byte sector of its own;
 //   * every spin-wait is bounded by state::spin_limit and reports through the
 //     error word instead of trapping (the reference traps, gallatin.cuh:87);
 //   * a vEB remove re-checks the emptied child word after clearing its
@@ -84,19 +91,42 @@ struct state {
   uint64_t *seg_tree;            // [veb.words]
   uint64_t *sub_trees;           // [num_trees * veb.words]
   uint16_t *tree_ids;            // [S]
-  int32_t *active;               // [S] blocks left to hand out, minus one
   uint32_t *qc;                  // [S] hand-out position
   uint32_t *qfc;                 // [S] return position
   uint32_t *fqfc;                // [S] finalised return position
-  unsigned long long *mwords;    // [S << bps_shift] (tree << 32) | count
-  uint32_t *fctr;                // [S << bps_shift] frees counted
+  unsigned long long *act;       // [S] (generation << 32) | (blocks left - 1 + ACT_BIAS)
+  unsigned long long *mwords;    // per block (tree << 32) | count, every mstride-th word
+  uint32_t *fctr;                // per block frees counted, every fstride-th word
+  uint32_t mstride;              // 4 with fstride 8: one 32-byte record per block
+  uint32_t fstride;              // 1 with fstride 1: dense arrays (gal_config.block_layout)
   uint32_t *queues;              // [S << bps_shift] recycle ring (block ids)
   uint32_t *slots;               // [total_slots] pinned blocks
   uint32_t *spares;              // [total_slots] next block per slot, prepared ahead
                                  // (gal_config.spare_blocks; NOBLK: none)
-  uint32_t *locks;               // tree locks (bit t) + bit num_trees for runs
+  uint32_t *locks;               // lock word of tree t at t * LOCK_STRIDE; runs at num_trees
   uint32_t *error;               // GAL_DEV_ERR_* bits
 };
+
+// ------------------------------------------------------------------ layout
+static constexpr uint32_t BLOCK_RECORD_BYTES = 32;  // block_layout 1: one sector per block
+static constexpr uint32_t LOCK_STRIDE = 8;          // u32 words between lock words (32 B)
+GAL_DEVICE_INLINE __host__ unsigned long long *mword_ptr(const state *s, uint32_t blk) {
+  return s->mwords + (uint64_t)blk * s->mstride;
+}
+GAL_DEVICE_INLINE __host__ uint32_t *fctr_ptr(const state *s, uint32_t blk) {
+  return s->fctr + (uint64_t)blk * s->fstride;
+}
+// A segment's count word: generation in the high half, the reference's
+// active count (blocks left to hand out minus one; -1 when none is left or the
+// segment is free) plus ACT_BIAS in the low half, so adding or subtracting one
+// never carries into the generation.
+static constexpr uint32_t ACT_BIAS = 0x80000000u;
+GAL_DEVICE_INLINE __host__ int32_t act_unbias(uint32_t low) { return (int32_t)(low - ACT_BIAS); }
+GAL_DEVICE_INLINE __host__ int32_t act_count(unsigned long long w) { return act_unbias((uint32_t)w); }
+GAL_DEVICE_INLINE __host__ uint32_t act_gen(unsigned long long w) { return (uint32_t)(w >> 32); }
+GAL_DEVICE_INLINE __host__ unsigned long long act_word(uint32_t gen, int32_t count) {
+  return ((unsigned long long)gen << 32) | (uint32_t)((uint32_t)count + ACT_BIAS);
+}
 
 // ------------------------------------------------------------------ helpers
 GAL_DEVICE_INLINE uint32_t lane_id() {
@@ -141,6 +171,9 @@ GAL_DEVICE_INLINE uint32_t ld_rlx(const uint32_t *p) {
 }
 GAL_DEVICE_INLINE int32_t ld_rlx(const int32_t *p) {
   return (int32_t)ld_rlx((const uint32_t *)p);
+}
+GAL_DEVICE_INLINE unsigned long long ld_rlx(const unsigned long long *p) {
+  return (unsigned long long)ld_rlx((const uint64_t *)p);
 }
 GAL_DEVICE_INLINE uint16_t ld_rlx(const uint16_t *p) {
   uint16_t v;
@@ -473,12 +506,14 @@ GAL_DEVICE_INLINE veb_ref sub_tree(const state *s, uint32_t t) {
 }
 
 // ------------------------------------------------------------------ locks
+// one lock word per class (and one for runs) in a 32-byte sector of its own;
+// the reference keeps them as bits of one word (gallatin.cuh:1513-1519)
 GAL_DEVICE_INLINE bool try_lock(const state *s, uint32_t bit) {
-  return (atomicOr(s->locks, 1u << bit) & (1u << bit)) == 0;  // gallatin.cuh:1513-1519
+  return atomicExch(s->locks + bit * LOCK_STRIDE, 1u) == 0u;
 }
 GAL_DEVICE_INLINE void unlock(const state *s, uint32_t bit) {
   __threadfence();
-  atomicAnd(s->locks, ~(1u << bit));
+  atomicExch(s->locks + bit * LOCK_STRIDE, 0u);
 }
 
 // ------------------------------------------------------------------ table
@@ -492,7 +527,11 @@ GAL_DEVICE_COLD bool setup_segment(const state *s, uint64_t seg, uint32_t tree) 
   atomicExch(&s->qc[seg], 0u);
   atomicExch(&s->qfc[seg], 0u);
   atomicExch(&s->fqfc[seg], 0u);
-  atomicExch(&s->active[seg], (int)nb - 1);
+  __threadfence();
+  // count -1 -> nb - 1 and a new generation, by addition: a reservation
+  // attempt still in flight from before the segment's release gives its one
+  // back into this count, as it took it from the count it found
+  atomicAdd(&s->act[seg], (1ull << 32) + nb);
   return true;
 }
 
@@ -510,30 +549,69 @@ GAL_DEVICE_COLD int64_t gather_new_segment(const state *s, uint32_t tree) {
   return (int64_t)seg;
 }
 
+// Releases segment `seg` of class `tree` when its count word still reads
+// `gen` with every block home (nb - 1): removes it from the class's tree,
+// frees its class and lists it in the segment tree (the release steps of
+// Gallatin::return_block, gallatin.cuh:1663-1722, finish_freeing_block,
+// memory_table.cuh:1226-1241).
+GAL_DEVICE_COLD void release_segment(const state *s, uint64_t seg, uint32_t tree, uint32_t gen, uint32_t nb) {
+  const unsigned long long home = act_word(gen, (int32_t)nb - 1);
+  if (atomicCAS(&s->act[seg], home, act_word(gen, -1)) != home) return;
+  __threadfence();
+  veb_remove(sub_tree(s, tree), seg);
+  __threadfence();
+  if (cas16(&s->tree_ids[seg], (uint16_t)tree, FREE_TREE) != (uint16_t)tree) set_error(s, GAL_DEV_ERR_SEGMENT_SETUP);
+  __threadfence();
+  veb_insert(seg_tree(s), seg);
+}
+
+// Gives back a reservation taken from segment `seg` that no block came of.
+// While it was held the count stayed below every-block-home, so no release
+// could run; if giving it back brings the count there and blocks were handed
+// out in this generation (every one of them has come home, the last return
+// having found the count one short), the segment is released here.  With no
+// hand-out yet the segment is a fresh one whose gatherer takes its first
+// block next, so it stays.
+GAL_DEVICE_COLD void give_back_reservation(const state *s, uint64_t seg) {
+  const unsigned long long old = atomicAdd(&s->act[seg], 1ull);
+  __threadfence();
+  const uint16_t tree = ld_rlx(&s->tree_ids[seg]);
+  if (tree >= s->num_trees) return;
+  const uint32_t nb = blocks_in_segment(s, tree);
+  if (act_count(old) + 1 == (int32_t)nb - 1 && ld_rlx(&s->qc[seg]) != 0)
+    release_segment(s, seg, tree, act_gen(old), nb);
+}
+
 // alloc_table::get_block (memory_table.cuh:915-993)
+// The reference subtracts one from the segment's count and adds it back when
+// the count went negative or the segment belongs to another class
+// (memory_table.cuh:923-929, get_slot_in_segment / return_slot_to_segment).
+// An add-back that lands after the segment was released and set up again
+// raises the new owner's count above its blocks, and one that lands after the
+// segment's last return leaves it unreleased.  Here the class is checked
+// against the count's generation before the subtraction, a count already
+// negative is not touched, and the subtraction carries into a new set-up (see
+// setup_segment), so the only give-backs left are the rare ones of a race
+// between the check and the subtraction, which give_back_reservation
+// settles.
 GAL_DEVICE_COLD uint32_t get_block(const state *s, uint64_t seg, uint32_t tree, bool &last) {
   last = false;
-  // Reserve one of the segment's blocks without ever taking the count below
-  // zero.  The reference subtracts and adds back on failure
-  // (memory_table.cuh:923-929, get_slot_in_segment / return_slot_to_segment);
-  // an add-back that lands after the segment was released and set up again
-  // raises the new count above the blocks the segment has, and later
-  // hand-outs then meet empty ring entries and releases come early.
-  int ac = ld_rlx(&s->active[seg]);
-  for (uint32_t i = 0;; i++) {
-    if (ac < 0) return NOBLK;
-    const int seen = atomicCAS(&s->active[seg], ac, ac - 1);
-    if (seen == ac) break;
-    ac = seen;
-    if (i >= s->spin_limit) {
-      set_error(s, GAL_DEV_ERR_TIMEOUT);
-      return NOBLK;
-    }
+  const unsigned long long seen = ld_rlx(&s->act[seg]);
+  if (act_count(seen) < 0) return NOBLK;  // nothing left (or a free segment)
+  __threadfence();
+  if (ld_rlx(&s->tree_ids[seg]) != (uint16_t)tree) return NOBLK;  // another class's segment
+  const unsigned long long old = atomicAdd(&s->act[seg], ~0ull);  // minus one
+  const int32_t ac = act_count(old);
+  if (ac < 0) {  // the last block went to another thread meanwhile
+    give_back_reservation(s, seg);
+    return NOBLK;
   }
   __threadfence();
-  if (ld_rlx(&s->tree_ids[seg]) != (uint16_t)tree) {
-    atomicAdd(&s->active[seg], 1);
-    __threadfence();
+  if (act_gen(old) != act_gen(seen) && ld_rlx(&s->tree_ids[seg]) != (uint16_t)tree) {
+    // released and set up for another class between the check and the
+    // subtraction; the class read now is the generation's own, as the
+    // reservation keeps it from being released
+    give_back_reservation(s, seg);
     return NOBLK;
   }
   uint32_t nb = blocks_in_segment(s, tree);
@@ -553,7 +631,7 @@ GAL_DEVICE_COLD uint32_t get_block(const state *s, uint64_t seg, uint32_t tree, 
       return NOBLK;
     }
   }
-  atomicExch(&s->mwords[blk], (unsigned long long)tree << 32);  // Block::init_malloc
+  atomicExch(mword_ptr(s, blk), (unsigned long long)tree << 32);  // Block::init_malloc
   if (ac == 0) last = true;
   return blk;
 }
@@ -633,31 +711,22 @@ GAL_DEVICE_COLD void return_block(const state *s, uint32_t blk) {
     veb_insert(sub_tree(s, tree), seg);
     __threadfence();
   }
-  int rid = atomicAdd(&s->active[seg], 1);
-  bool release = false;
-  if ((uint32_t)(rid + 2) == nb) {  // all_blocks_free: rid == nb - 2
-    release = atomicCAS(&s->active[seg], (int)nb - 1, -1) == (int)nb - 1;
-  }
+  const unsigned long long old = atomicAdd(&s->act[seg], 1ull);
   __threadfence();
-  if (release) {
-    veb_remove(sub_tree(s, tree), seg);
-    __threadfence();
-    if (cas16(&s->tree_ids[seg], tree, FREE_TREE) != tree) set_error(s, GAL_DEV_ERR_SEGMENT_SETUP);
-    __threadfence();
-    veb_insert(seg_tree(s), seg);
-  }
+  if ((uint32_t)(act_count(old) + 2) == nb)  // all_blocks_free: the count was nb - 2
+    release_segment(s, seg, tree, act_gen(old), nb);
 }
 
 // Block::block_free_multiple + reset_free + free_block (block.cuh:87-98,200-212,
 // gallatin.cuh:1732-1766)
 GAL_DEVICE_INLINE void credit_done(const state *s, uint32_t blk, uint32_t old, uint32_t n);
 GAL_DEVICE_INLINE void credit_frees(const state *s, uint32_t blk, uint32_t n) {
-  credit_done(s, blk, atomicAdd(&s->fctr[blk], n), n);
+  credit_done(s, blk, atomicAdd(fctr_ptr(s, blk), n), n);
 }
 // the block's free counter was `old` before this thread added n
 GAL_DEVICE_INLINE void credit_done(const state *s, uint32_t blk, uint32_t old, uint32_t n) {
   if (old + n == SLICES_PER_BLOCK) {
-    atomicExch(&s->fctr[blk], 0u);
+    atomicExch(fctr_ptr(s, blk), 0u);
     __threadfence();
     return_block(s, blk);
   } else if (old + n > SLICES_PER_BLOCK) {
@@ -797,7 +866,7 @@ GAL_DEVICE_INLINE void *malloc_slices(const state *s, uint32_t tree, uint32_t co
         }
       }
       unsigned long long old = 0;
-      if ((int)lane == last) old = atomicAdd(&s->mwords[blk], (unsigned long long)total);
+      if ((int)lane == last) old = atomicAdd(mword_ptr(s, blk), (unsigned long long)total);
       old = __shfl_sync(live, old, last);
       const uint64_t alloc = (old & 0xFFFFFFFFull) + prefix;
       const bool start_valid = alloc <= SLICES_PER_BLOCK - 1;
@@ -832,10 +901,10 @@ GAL_DEVICE_COLD void *malloc_whole_block(const state *s, uint32_t tree) {
   for (int a = 0; a < BLOCK_ATTEMPTS; a++) {
     uint32_t blk = request_block(s, tree, tid);
     if (blk == NOBLK) return nullptr;
-    unsigned long long old = atomicAdd(&s->mwords[blk], (unsigned long long)SLICES_PER_BLOCK);
+    unsigned long long old = atomicAdd(mword_ptr(s, blk), (unsigned long long)SLICES_PER_BLOCK);
     uint32_t old_count = (uint32_t)old;
     if ((uint32_t)(old >> 32) != tree) set_error(s, GAL_DEV_ERR_BLOCK_TREE);
-    atomicAdd(&s->fctr[blk], (SLICES_PER_BLOCK - 1) - old_count);
+    atomicAdd(fctr_ptr(s, blk), (SLICES_PER_BLOCK - 1) - old_count);
     if (old_count != 0) {
       credit_frees(s, blk, 1);
       continue;
@@ -1002,11 +1071,17 @@ GAL_DEVICE_INLINE void free_n(const state *s, void *const (&p)[N], const bool (&
     const uint32_t team = __match_any_sync(active, blk[k]) & team_group(s);
     lead[k] = (int)lane_id() == __ffs(team) - 1;
     cnt[k] = (uint32_t)__popc(team);
-    if (lead[k]) old[k] = atomicAdd(&s->fctr[blk[k]], cnt[k]);
+    if (lead[k]) old[k] = atomicAdd(fctr_ptr(s, blk[k]), cnt[k]);
   }
 #pragma unroll
   for (int k = 0; k < N; k++)
     if (lead[k]) credit_done(s, blk[k], old[k], cnt[k]);
+}
+
+// a block's malloc word in the reference packing, (tree << 20) + count (block.cuh:53,220)
+GAL_DEVICE_INLINE uint32_t export_mword(const state *s, uint32_t blk) {
+  const unsigned long long w = *mword_ptr(s, blk);
+  return (uint32_t)(((w >> 32) << 20) + (w & 0xFFFFFFFFull));
 }
 
 // bytes a request of `size` occupies (Gallatin::get_allocated_size, gallatin.cuh:1152-1183)

@@ -31,6 +31,9 @@ using namespace gallatin::allocators;
 #endif
 
 using ref_type = Gallatin<REF_SEGMENT_BYTES, REF_MIN_SIZE, REF_MAX_SIZE>;
+
+// the template arguments this cubin was built with (read by ref_loader.c)
+extern "C" __device__ uint64_t ref_geometry[3] = {REF_SEGMENT_BYTES, REF_MIN_SIZE, REF_MAX_SIZE};
 using table_type = alloc_table<REF_SEGMENT_BYTES, REF_MIN_SIZE>;
 using pinned_type = pinned_shared_blocks<REF_MIN_SIZE, REF_MAX_SIZE>;
 
@@ -350,4 +353,19 @@ extern "C" __global__ void ref_stamp_free(ref_type *a, uint64_t n, uint64_t **pt
   }
   galwl::warp_count(&stats[2], bad);
   galwl::warp_count(&stats[3], p != nullptr);
+}
+
+// one thread per request through the reference's per-thread malloc / free
+// (global_malloc / global_free, global_allocator.cuh:72-82, on a handle)
+extern "C" __global__ void ref_malloc_sizes(ref_type *a, const uint64_t *sizes, uint64_t n, void **out) {
+  uint64_t tid = gallatin::utils::get_tid();
+  if (tid >= n) return;
+  out[tid] = a->malloc(sizes[tid]);
+}
+
+extern "C" __global__ void ref_free_ptrs(ref_type *a, void *const *ptrs, uint64_t n) {
+  uint64_t tid = gallatin::utils::get_tid();
+  if (tid >= n) return;
+  void *p = ptrs[tid];
+  if (p) a->free(p);
 }

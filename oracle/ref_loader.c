@@ -1,10 +1,11 @@
 /*
  * ref_loader.c — host side of the reference harness (TEST INFRASTRUCTURE ONLY).
  *
- * Loads oracle/_ref/ref_harness.cubin (the reference's own device code compiled
- * from its sources) through the CUDA driver API and exposes a small C ABI used
- * by oracle/refgpu.py: build + boot an instance, replay a serial trace, export
- * the state in the gal_state_view layout, and time the churn / stamp workloads.
+ * Loads oracle/_ref/ref_harness*.cubin (the reference's own device code compiled
+ * from its sources, one cubin per segment size) through the CUDA driver API and
+ * exposes a small C ABI used by oracle/refgpu.py: build + boot an instance,
+ * replay a serial trace, export the state in the gal_state_view layout, serve
+ * request batches, and time the churn / stamp workloads.
  */
 #include <cuda.h>
 #include <stdint.h>
@@ -26,42 +27,86 @@
   } while (0)
 
 static CUcontext g_ctx;
-static CUmodule g_mod;
-static unsigned g_free_grid; /* persistent grid of ref_churn_free: SMs x resident CTAs */
-static CUfunction f_build, f_boot1, f_bootr, f_replay, f_replay_warp, f_export, f_cmalloc, f_cfree, f_smalloc, f_sfree;
-static int g_open = 0;
+static int g_init = 0;
+
+/* one loaded cubin: the reference built for one Gallatin<seg, min, max> */
+typedef struct {
+  char path[1024];
+  CUmodule mod;
+  unsigned free_grid; /* persistent grid of ref_churn_free: SMs x resident CTAs */
+  uint64_t seg_bytes, min_size, max_size;
+  CUfunction f_build, f_boot1, f_bootr, f_replay, f_replay_warp, f_export, f_cmalloc, f_cfree, f_smalloc,
+      f_sfree, f_malloc_n, f_free_n;
+} ref_mod;
+
+#define MAX_MODS 4
+static ref_mod g_mods[MAX_MODS];
+static int g_nmods = 0;
 
 typedef struct {
+  const ref_mod *m;
   CUdeviceptr arena, scratch, alloc_ptr_buf, status;
   uint64_t num_bytes, scratch_bytes;
   CUdeviceptr alloc; /* device address of the Gallatin object */
 } ref_inst;
 
+/* Loads a harness cubin (once per path); returns its module id (>= 0) or a
+ * negative error. */
 int ref_open(const char *cubin) {
-  if (g_open) return 0;
+  for (int i = 0; i < g_nmods; i++)
+    if (strcmp(g_mods[i].path, cubin) == 0) return i;
+  if (g_nmods == MAX_MODS || strlen(cubin) >= sizeof(g_mods[0].path)) return -1;
   CUdevice d;
-  CK(cuInit(0));
-  CK(cuDeviceGet(&d, 0));
-  CK(cuDevicePrimaryCtxRetain(&g_ctx, d));
+  if (!g_init) {
+    CK(cuInit(0));
+    CK(cuDeviceGet(&d, 0));
+    CK(cuDevicePrimaryCtxRetain(&g_ctx, d));
+    g_init = 1;
+  }
   CK(cuCtxSetCurrent(g_ctx));
-  CK(cuModuleLoad(&g_mod, cubin));
-  CK(cuModuleGetFunction(&f_build, g_mod, "ref_build"));
-  CK(cuModuleGetFunction(&f_boot1, g_mod, "ref_boot_one_thread"));
-  CK(cuModuleGetFunction(&f_bootr, g_mod, "ref_boot_racy"));
-  CK(cuModuleGetFunction(&f_replay, g_mod, "ref_replay"));
-  CK(cuModuleGetFunction(&f_replay_warp, g_mod, "ref_replay_warp"));
-  CK(cuModuleGetFunction(&f_export, g_mod, "ref_export"));
-  CK(cuModuleGetFunction(&f_cmalloc, g_mod, "ref_churn_malloc"));
-  CK(cuModuleGetFunction(&f_cfree, g_mod, "ref_churn_free"));
-  CK(cuModuleGetFunction(&f_smalloc, g_mod, "ref_stamp_malloc"));
-  CK(cuModuleGetFunction(&f_sfree, g_mod, "ref_stamp_free"));
+  CK(cuDeviceGet(&d, 0));
+  ref_mod *m = &g_mods[g_nmods];
+  memset(m, 0, sizeof(*m));
+  strcpy(m->path, cubin);
+  CK(cuModuleLoad(&m->mod, cubin));
+  CK(cuModuleGetFunction(&m->f_build, m->mod, "ref_build"));
+  CK(cuModuleGetFunction(&m->f_boot1, m->mod, "ref_boot_one_thread"));
+  CK(cuModuleGetFunction(&m->f_bootr, m->mod, "ref_boot_racy"));
+  CK(cuModuleGetFunction(&m->f_replay, m->mod, "ref_replay"));
+  CK(cuModuleGetFunction(&m->f_replay_warp, m->mod, "ref_replay_warp"));
+  CK(cuModuleGetFunction(&m->f_export, m->mod, "ref_export"));
+  CK(cuModuleGetFunction(&m->f_cmalloc, m->mod, "ref_churn_malloc"));
+  CK(cuModuleGetFunction(&m->f_cfree, m->mod, "ref_churn_free"));
+  CK(cuModuleGetFunction(&m->f_smalloc, m->mod, "ref_stamp_malloc"));
+  CK(cuModuleGetFunction(&m->f_sfree, m->mod, "ref_stamp_free"));
+  CK(cuModuleGetFunction(&m->f_malloc_n, m->mod, "ref_malloc_sizes"));
+  CK(cuModuleGetFunction(&m->f_free_n, m->mod, "ref_free_ptrs"));
+  {
+    CUdeviceptr gp;
+    size_t gb = 0;
+    uint64_t geo[3];
+    CK(cuModuleGetGlobal(&gp, &gb, m->mod, "ref_geometry"));
+    if (gb != sizeof(geo)) return -2;
+    CK(cuMemcpyDtoH(geo, gp, sizeof(geo)));
+    m->seg_bytes = geo[0];
+    m->min_size = geo[1];
+    m->max_size = geo[2];
+  }
   {
     int sms = 0, per_sm = 0;
     CK(cuDeviceGetAttribute(&sms, CU_DEVICE_ATTRIBUTE_MULTIPROCESSOR_COUNT, d));
-    CK(cuOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f_cfree, 256, 0));
-    g_free_grid = (unsigned)(sms * (per_sm > 0 ? per_sm : 1));
+    CK(cuOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, m->f_cfree, 256, 0));
+    m->free_grid = (unsigned)(sms * (per_sm > 0 ? per_sm : 1));
   }
-  g_open = 1;
+  return g_nmods++;
+}
+
+/* the geometry a module was built for: bytes per segment, min and max slice */
+int ref_module_geometry(int mod, uint64_t *out3) {
+  if (mod < 0 || mod >= g_nmods || !out3) return -1;
+  out3[0] = g_mods[mod].seg_bytes;
+  out3[1] = g_mods[mod].min_size;
+  out3[2] = g_mods[mod].max_size;
   return 0;
 }
 
@@ -71,21 +116,26 @@ static int launch(CUfunction f, unsigned grid, unsigned block, void **args) {
 }
 
 /* boot_mode: 0 none, 1 one-thread order, 2 the reference's racy <<<1,128>>> */
-int ref_create(uint64_t num_bytes, uint64_t seed, int boot_mode, void **out) {
-  if (!g_open) return -1;
-  ref_inst *r = (ref_inst *)calloc(1, sizeof(ref_inst));
-  uint64_t S = num_bytes / (16ULL << 20);
+int ref_create(int mod, uint64_t num_bytes, uint64_t seed, int boot_mode, void **out) {
+  if (mod < 0 || mod >= g_nmods) return -1;
+  const ref_mod *m = &g_mods[mod];
+  CK(cuCtxSetCurrent(g_ctx));
+  uint64_t S = num_bytes / m->seg_bytes;
   if (S == 0) return -2;
+  const uint64_t bps = m->seg_bytes / (m->min_size * 4096);
+  ref_inst *r = (ref_inst *)calloc(1, sizeof(ref_inst));
+  r->m = m;
   r->num_bytes = num_bytes;
-  r->scratch_bytes = S * 256 * 16 + (8ULL << 20);
-  CK(cuMemAlloc(&r->arena, S * (16ULL << 20)));
-  CK(cuMemsetD8(r->arena, 0, S * (16ULL << 20)));
+  /* Block (8 B) and queue entry (8 B) per block, plus trees and slots */
+  r->scratch_bytes = S * bps * 16 + (8ULL << 20);
+  CK(cuMemAlloc(&r->arena, S * m->seg_bytes));
+  CK(cuMemsetD8(r->arena, 0, S * m->seg_bytes));
   CK(cuMemAlloc(&r->scratch, r->scratch_bytes));
   CK(cuMemAlloc(&r->alloc_ptr_buf, 8));
   CK(cuMemAlloc(&r->status, 16));
   void *args[] = {&r->scratch, &r->scratch_bytes, &r->arena, &num_bytes, &seed, &r->alloc_ptr_buf,
                   &r->status};
-  int e = launch(f_build, 1, 1, args);
+  int e = launch(m->f_build, 1, 1, args);
   if (e) return e;
   CK(cuCtxSynchronize());
   uint64_t st[2];
@@ -97,11 +147,11 @@ int ref_create(uint64_t num_bytes, uint64_t seed, int boot_mode, void **out) {
   CK(cuMemcpyDtoH(&r->alloc, r->alloc_ptr_buf, 8));
   if (boot_mode == 1) {
     void *a2[] = {&r->alloc};
-    e = launch(f_boot1, 1, 1, a2);
+    e = launch(m->f_boot1, 1, 1, a2);
     if (e) return e;
   } else if (boot_mode == 2) {
     void *a2[] = {&r->alloc};
-    e = launch(f_bootr, 1, 128, a2);
+    e = launch(m->f_bootr, 1, 128, a2);
     if (e) return e;
   }
   CK(cuCtxSynchronize());
@@ -132,7 +182,7 @@ int ref_replay(void *h, const uint64_t *ops, uint64_t n, uint64_t *out, uint32_t
   CK(cuMemcpyHtoD(d_ops, ops, n * 8));
   CK(cuMemsetD8(d_out, 0xFF, n * 8));
   void *args[] = {&r->alloc, &d_ops, &n, &d_out, &d_smid};
-  int e = launch(f_replay, 1, 1, args);
+  int e = launch(r->m->f_replay, 1, 1, args);
   if (e) return e;
   CK(cuCtxSynchronize());
   CK(cuMemcpyDtoH(out, d_out, n * 8));
@@ -153,7 +203,7 @@ int ref_replay_warp(void *h, const uint64_t *steps, uint64_t nsteps, uint64_t *o
   CK(cuMemcpyHtoD(d_steps, steps, nsteps * 33 * 8));
   CK(cuMemsetD8(d_out, 0xFF, nsteps * 32 * 8));
   void *args[] = {&r->alloc, &d_steps, &nsteps, &d_out, &d_smid};
-  int e = launch(f_replay_warp, 1, 32, args);
+  int e = launch(r->m->f_replay_warp, 1, 32, args);
   if (e) return e;
   CK(cuCtxSynchronize());
   CK(cuMemcpyDtoH(out, d_out, nsteps * 32 * 8));
@@ -191,7 +241,7 @@ int ref_export(void *h, const gal_state_dims *d, gal_state_view *v) {
   CK(cuMemAlloc(&p.locks, 8));
   p.veb_words = W;
   void *args[] = {&r->alloc, &p};
-  int e = launch(f_export, 152, 256, args);
+  int e = launch(r->m->f_export, 152, 256, args);
   if (e) return e;
   CK(cuCtxSynchronize());
   CK(cuMemcpyDtoH(v->seg_tree_words, p.seg_tree_words, W * 8));
@@ -215,9 +265,9 @@ int ref_export(void *h, const gal_state_dims *d, gal_state_view *v) {
 }
 
 /* the free phase is persistent: one warp per 1,024 slots at a time (churn.cuh) */
-static unsigned free_grid(uint64_t nscan) {
+static unsigned free_grid(const ref_mod *m, uint64_t nscan) {
   uint64_t need = (nscan + 8 * 1024 - 1) / (8 * 1024);
-  return (unsigned)(need < g_free_grid ? need : g_free_grid);
+  return (unsigned)(need < m->free_grid ? need : m->free_grid);
 }
 
 /* Mixed-size churn, `steps` timed steps after `warmup` untimed ones.  One step:
@@ -250,19 +300,19 @@ int ref_churn(void *h, uint64_t threads_per_round, uint32_t rounds, uint32_t see
         uint64_t nscan = threads_per_round * rd;
         int all = 0;
         void *fa[] = {&r->alloc, &ptrs, &live, &nscan, &rd, &seed, &all, &stats};
-        int e = launch(f_cfree, free_grid(nscan), block, fa);
+        int e = launch(r->m->f_cfree, free_grid(r->m, nscan), block, fa);
         if (e) return e;
       }
       uint64_t base = threads_per_round * rd;
       void *ma[] = {&r->alloc, &ptrs, &live, &base, &threads_per_round, &seed, &stats};
-      int e = launch(f_cmalloc, (unsigned)((threads_per_round + block - 1) / block), block, ma);
+      int e = launch(r->m->f_cmalloc, (unsigned)((threads_per_round + block - 1) / block), block, ma);
       if (e) return e;
     }
     {
       int all = 1;
       uint32_t rd = rounds;
       void *fa[] = {&r->alloc, &ptrs, &live, &nslots, &rd, &seed, &all, &stats};
-      int e = launch(f_cfree, free_grid(nslots), block, fa);
+      int e = launch(r->m->f_cfree, free_grid(r->m, nslots), block, fa);
       if (e) return e;
     }
     CK(cuEventRecord(e1, 0));
@@ -305,10 +355,10 @@ int ref_stamp(void *h, uint64_t n, uint64_t size, int rounds, float *out_ms,
     void *ma[] = {&r->alloc, &n, &size, &ptrs, &stats};
     void *fa[] = {&r->alloc, &n, &ptrs, &stats};
     CK(cuEventRecord(e0, 0));
-    int e = launch(f_smalloc, grid, block, ma);
+    int e = launch(r->m->f_smalloc, grid, block, ma);
     if (e) return e;
     CK(cuEventRecord(e1, 0));
-    e = launch(f_sfree, grid, block, fa);
+    e = launch(r->m->f_sfree, grid, block, fa);
     if (e) return e;
     CK(cuEventRecord(e2, 0));
     CK(cuEventSynchronize(e2));
@@ -321,5 +371,56 @@ int ref_stamp(void *h, uint64_t n, uint64_t size, int rounds, float *out_ms,
   CK(cuMemcpyDtoH(stats_out, stats, 32));
   CK(cuMemFree(ptrs));
   CK(cuMemFree(stats));
+  return 0;
+}
+
+/* One device thread per request: out[i] = malloc(sizes[i]) through the
+ * reference's per-thread malloc; host arrays in and out.  *ms: kernel time
+ * (CUDA events around the launch). */
+int ref_malloc_sizes(void *h, const uint64_t *sizes, uint64_t n, uint64_t *out, float *ms) {
+  ref_inst *r = (ref_inst *)h;
+  if (!n) return 0;
+  CUdeviceptr d_sizes, d_out;
+  CK(cuMemAlloc(&d_sizes, n * 8));
+  CK(cuMemAlloc(&d_out, n * 8));
+  CK(cuMemcpyHtoD(d_sizes, sizes, n * 8));
+  CUevent e0, e1;
+  CK(cuEventCreate(&e0, CU_EVENT_DEFAULT));
+  CK(cuEventCreate(&e1, CU_EVENT_DEFAULT));
+  void *args[] = {&r->alloc, &d_sizes, &n, &d_out};
+  CK(cuEventRecord(e0, 0));
+  int e = launch(r->m->f_malloc_n, (unsigned)((n + 255) / 256), 256, args);
+  if (e) return e;
+  CK(cuEventRecord(e1, 0));
+  CK(cuEventSynchronize(e1));
+  CK(cuEventElapsedTime(ms, e0, e1));
+  CK(cuMemcpyDtoH(out, d_out, n * 8));
+  CK(cuEventDestroy(e0));
+  CK(cuEventDestroy(e1));
+  CK(cuMemFree(d_sizes));
+  CK(cuMemFree(d_out));
+  return 0;
+}
+
+/* One device thread per pointer: free(ptrs[i]) unless 0; host array in. */
+int ref_free_ptrs(void *h, const uint64_t *ptrs, uint64_t n, float *ms) {
+  ref_inst *r = (ref_inst *)h;
+  if (!n) return 0;
+  CUdeviceptr d_ptrs;
+  CK(cuMemAlloc(&d_ptrs, n * 8));
+  CK(cuMemcpyHtoD(d_ptrs, ptrs, n * 8));
+  CUevent e0, e1;
+  CK(cuEventCreate(&e0, CU_EVENT_DEFAULT));
+  CK(cuEventCreate(&e1, CU_EVENT_DEFAULT));
+  void *args[] = {&r->alloc, &d_ptrs, &n};
+  CK(cuEventRecord(e0, 0));
+  int e = launch(r->m->f_free_n, (unsigned)((n + 255) / 256), 256, args);
+  if (e) return e;
+  CK(cuEventRecord(e1, 0));
+  CK(cuEventSynchronize(e1));
+  CK(cuEventElapsedTime(ms, e0, e1));
+  CK(cuEventDestroy(e0));
+  CK(cuEventDestroy(e1));
+  CK(cuMemFree(d_ptrs));
   return 0;
 }

@@ -16,14 +16,18 @@ from gallatin_gb300._abi import FAIL, GalStateDims, StateView
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
-CUBIN = os.path.join(REF_DIR, "ref_harness.cubin")
+# the reference built as Gallatin<seg, 16, 4096>, one cubin per segment size
+CUBINS = {16: os.path.join(REF_DIR, "ref_harness.cubin"),
+          64: os.path.join(REF_DIR, "ref_harness_64m.cubin")}
+CUBIN = CUBINS[16]
 LOADER = os.path.join(REF_DIR, "libref_loader.so")
 
 _lib = None
+_mods = {}
 
 
-def available():
-    return os.path.exists(CUBIN)
+def available(segment_mib=16):
+    return os.path.exists(CUBINS[segment_mib])
 
 
 def _build_loader():
@@ -41,7 +45,10 @@ def lib():
         _build_loader()
         L = C.CDLL(LOADER)
         L.ref_open.argtypes = [C.c_char_p]
-        L.ref_create.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.POINTER(C.c_void_p)]
+        L.ref_module_geometry.argtypes = [C.c_int, C.c_void_p]
+        L.ref_create.argtypes = [C.c_int, C.c_uint64, C.c_uint64, C.c_int, C.POINTER(C.c_void_p)]
+        L.ref_malloc_sizes.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]
+        L.ref_free_ptrs.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
         L.ref_destroy.argtypes = [C.c_void_p]
         L.ref_replay.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]
         L.ref_replay_warp.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]
@@ -51,26 +58,59 @@ def lib():
         L.ref_stamp.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64, C.c_int, C.c_void_p, C.c_void_p]
         L.ref_arena_base.restype = C.c_uint64
         L.ref_arena_base.argtypes = [C.c_void_p]
-        r = L.ref_open(CUBIN.encode())
-        if r != 0:
-            raise RuntimeError(f"ref_open failed ({r})")
         _lib = L
     return _lib
+
+
+def module(segment_mib=16):
+    """Module id of the cubin built for segment_mib MiB segments (loaded once)."""
+    if segment_mib not in _mods:
+        if not available(segment_mib):
+            raise FileNotFoundError(f"{CUBINS[segment_mib]} missing")
+        r = lib().ref_open(CUBINS[segment_mib].encode())
+        if r < 0:
+            raise RuntimeError(f"ref_open failed ({r})")
+        _mods[segment_mib] = r
+    return _mods[segment_mib]
 
 
 BOOT_NONE, BOOT_ONE_THREAD, BOOT_RACY = 0, 1, 2
 
 
 class RefGPU:
-    """One instance of the reference's Gallatin<16 MiB, 16, 4096> on the GPU."""
+    """One instance of the reference's Gallatin<segment_mib MiB, 16, 4096> on the GPU."""
 
-    def __init__(self, num_bytes, seed, boot=BOOT_ONE_THREAD):
+    def __init__(self, num_bytes, seed, boot=BOOT_ONE_THREAD, segment_mib=16):
         h = C.c_void_p()
-        r = lib().ref_create(num_bytes, seed, boot, C.byref(h))
+        r = lib().ref_create(module(segment_mib), num_bytes, seed, boot, C.byref(h))
         if r != 0:
             raise RuntimeError(f"ref_create failed ({r})")
         self._h = h
         self.num_bytes = num_bytes
+        self.segment_bytes = segment_mib << 20
+
+    @property
+    def arena_base(self):
+        return int(lib().ref_arena_base(self._h))
+
+    def malloc_sizes(self, sizes):
+        """One device thread per request (host array in); returns (pointers, kernel ms)."""
+        sizes = np.ascontiguousarray(sizes, dtype=np.uint64)
+        out = np.zeros(len(sizes), dtype=np.uint64)
+        ms = C.c_float()
+        r = lib().ref_malloc_sizes(self._h, sizes.ctypes.data, len(sizes), out.ctypes.data, C.byref(ms))
+        if r != 0:
+            raise RuntimeError(f"ref_malloc_sizes failed ({r})")
+        return out, ms.value
+
+    def free_ptrs(self, ptrs):
+        """One device thread per pointer (0 skipped); returns the kernel ms."""
+        ptrs = np.ascontiguousarray(ptrs, dtype=np.uint64)
+        ms = C.c_float()
+        r = lib().ref_free_ptrs(self._h, ptrs.ctypes.data, len(ptrs), C.byref(ms))
+        if r != 0:
+            raise RuntimeError(f"ref_free_ptrs failed ({r})")
+        return ms.value
 
     def close(self):
         if self._h:
@@ -122,3 +162,38 @@ class RefGPU:
         if r != 0:
             raise RuntimeError(f"ref_stamp failed ({r})")
         return ms, st
+
+
+class LargeBlockBackend:
+    """The reference build as a backend of
+    gallatin_gb300.workloads.large_block_workload: per-thread malloc/free of
+    request batches, and the free runs of its segment tree for the
+    fragmentation figure."""
+
+    def __init__(self, ref: RefGPU, seed):
+        from oracle.oracle import Oracle
+        self.ref = ref
+        self.arena_bytes = ref.num_bytes // ref.segment_bytes * ref.segment_bytes
+        self.arena_base = ref.arena_base
+        self.dims = Oracle(ref.num_bytes, seed, boot=False).dims()
+
+    def malloc(self, sizes):
+        return self.ref.malloc_sizes(sizes)
+
+    def free(self, ptrs):
+        return self.ref.free_ptrs(np.asarray(ptrs).view(np.uint64))
+
+    def free_runs(self):
+        from gallatin_gb300.workloads import largest_run_of_ones
+        sv = self.ref.export(self.dims)
+        S = int(self.dims.num_segments)
+        bottom = sv.seg_tree_words[-((S + 63) // 64):]
+        free = int(sum(bin(int(w)).count("1") for w in bottom))
+        return largest_run_of_ones(bottom, S), free
+
+    def extra(self):
+        sv = self.ref.export(self.dims)
+        T = int(self.dims.num_trees)
+        ids = sv.tree_ids.astype(np.int64)
+        return {"multi_segment_allocs_after_drain": int(((ids > T) & (ids != 0xFFFF)).sum()),
+                "error_word": None}

@@ -527,3 +527,56 @@ extern "C" int dropin_calloc_test(uint64_t num_bytes, uint64_t n, int rounds, in
   out[3] = err;
   return e == cudaSuccess ? 0 : 1;
 }
+
+// ---- a global handle that is not set: global_malloc returns nullptr and
+// global_free does nothing (the reference's failure contract,
+// global_allocator.cuh:72-82), in a translation unit that never called
+// init_global_allocator or after free_global_allocator cleared the handle
+
+__global__ void null_handle_calls(uint64_t n, uint64_t size, void *stale, unsigned long long *c) {
+  uint64_t tid = threadIdx.x + (uint64_t)blockIdx.x * blockDim.x;
+  if (tid >= n) return;
+  void *p = global_malloc(size);
+  void *q = global_malloc_host(size);
+  if (p != nullptr) atomicAdd(c, 1ull);
+  if (q != nullptr) atomicAdd(c + 1, 1ull);
+  global_free(stale);       // no instance: nothing to give it back to
+  global_free_host(stale);
+  if (global_malloc_poison(size) != nullptr) atomicAdd(c + 2, 1ull);
+}
+
+__global__ void one_malloc(uint64_t size, void **out) { out[0] = global_malloc(size); }
+
+// out[0] non-null results before any init, out[1] non-null host results,
+// out[2] non-null poison results, out[3] whether the initialised instance
+// served (1), out[4] non-null results after free_global_allocator
+extern "C" int dropin_null_handle_test(uint64_t n, uint64_t *out) {
+  unsigned long long *c = nullptr;
+  void **slot = nullptr;
+  cudaMalloc(&c, 3 * sizeof(unsigned long long));
+  cudaMalloc(&slot, sizeof(void *));
+  cudaMemset(c, 0, 3 * sizeof(unsigned long long));
+  unsigned grid = (unsigned)((n + 255) / 256);
+  null_handle_calls<<<grid, 256>>>(n, 64, nullptr, c);
+  cudaError_t e = cudaDeviceSynchronize();
+  unsigned long long h[3] = {0, 0, 0};
+  cudaMemcpy(h, c, sizeof(h), cudaMemcpyDeviceToHost);
+  out[0] = h[0];
+  out[1] = h[1];
+  out[2] = h[2];
+  init_global_allocator(1ull << 30, 42, false);
+  one_malloc<<<1, 1>>>(64, slot);
+  void *served = nullptr;
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  cudaMemcpy(&served, slot, sizeof(void *), cudaMemcpyDeviceToHost);
+  out[3] = served != nullptr;
+  free_global_allocator();
+  cudaMemset(c, 0, 3 * sizeof(unsigned long long));
+  null_handle_calls<<<grid, 256>>>(n, 64, served, c);  // `served` now dangles: the free ignores it
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  cudaMemcpy(h, c, sizeof(h), cudaMemcpyDeviceToHost);
+  out[4] = h[0] + h[1] + h[2];
+  cudaFree(c);
+  cudaFree(slot);
+  return e == cudaSuccess ? 0 : 1;
+}

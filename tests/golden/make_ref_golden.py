@@ -46,6 +46,18 @@ def exhaust_trace():
     return np.array(ops, dtype=np.uint64)
 
 
+def hidden_by_return_trace():
+    """On 128 segments with no pinned blocks: a run of 34 segments (94-127), a
+    run of 36 (58-93, which empties bottom word 1 of the segment tree), the
+    second run freed (word 1 refilled with 64-93 but not full), then 100 whole
+    16 MiB blocks.  The reference lists a refilled word in the summary layer
+    only when it is full (veb.cuh:1128-1154), so its single-segment searches
+    reach 64 of them; with every refilled word listed, 94."""
+    seg = 16 << 20
+    ops = [34 * seg, 36 * seg, (1 << 63) | 1] + [seg] * 100
+    return np.array(ops, dtype=np.uint64)
+
+
 CASES = [
     # name, arena bytes, alloc seed, boot, trace builder
     ("cfg1_serial", 2 * GiB, 42, refgpu.BOOT_ONE_THREAD, lambda: gen_serial_trace(7, 4096, 60, 16, 256)),
@@ -55,7 +67,12 @@ CASES = [
     ("tiers", 16 * GiB, 42, refgpu.BOOT_ONE_THREAD, lambda: gen_log_trace(17, 3000, 55, 4, 26)),
     ("exhaust_4k", 256 << 20, 42, refgpu.BOOT_ONE_THREAD, exhaust_trace),
     ("cfg1_racy_boot", 2 * GiB, 42, refgpu.BOOT_RACY, lambda: gen_serial_trace(7, 4096, 60, 16, 256)),
+    ("run_return_hidden", 2 * GiB, 42, refgpu.BOOT_NONE, hidden_by_return_trace),
 ]
+
+# cases whose trace reaches a reference defect that the product fixes: the
+# product's offsets differ there by design
+REACHES_FIX = {"run_return_hidden": "FIX_RUN_RETURN_SUMMARY"}
 
 
 WARP_CASES = [
@@ -130,6 +147,8 @@ def main():
                        "mallocs": int((ops < (1 << 63)).sum()),
                        "failed_mallocs": int(((ops < (1 << 63)) & (offsets == (1 << 64) - 1)).sum()),
                        "seconds": round(time.time() - t0, 2)}
+        if name in REACHES_FIX:
+            index[name]["reaches_fix"] = REACHES_FIX[name]
         print(name, index[name], flush=True)
     if index:
         _merge_index(os.path.join(out_dir, "index.json"), index)

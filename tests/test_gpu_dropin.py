@@ -142,3 +142,15 @@ def test_calloc_mode_hands_out_zeroed_memory(D, calloc_mode):
         assert out[1] == 0
     else:
         assert out[1] > 0
+
+
+def test_unset_global_handle_returns_null(D):
+    """A global handle that was never set in the caller's translation unit, or
+    was cleared by free_global_allocator, gives nullptr from global_malloc (and
+    from the host and poison variants) and a global_free that does nothing;
+    between the two, the initialised instance serves."""
+    D.dropin_null_handle_test.argtypes = [C.c_uint64, C.c_void_p]
+    D.dropin_null_handle_test.restype = C.c_int
+    out = np.zeros(5, dtype=np.uint64)
+    assert D.dropin_null_handle_test(4096, out.ctypes.data) == 0
+    assert out.tolist() == [0, 0, 0, 1, 0]

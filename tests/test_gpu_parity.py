@@ -38,7 +38,7 @@ def _golden(name):
     return boot, final, z["ops"], z["offsets"], int(z["smid"][0])
 
 
-@pytest.mark.parametrize("name", sorted(INDEX))
+@pytest.mark.parametrize("name", sorted(n for n in INDEX if "reaches_fix" not in INDEX[n]))
 def test_serial_trace_matches_reference_build(G, name):
     meta = INDEX[name]
     boot, final, ops, offsets, smid = _golden(name)
@@ -53,6 +53,26 @@ def test_serial_trace_matches_reference_build(G, name):
         out, _ = g.replay(ops)
         np.testing.assert_array_equal(out, offsets)
         assert g.export().diff(final) == [], "final state differs from the reference build"
+        assert g.error_word() == 0
+    finally:
+        g.close()
+
+
+@pytest.mark.parametrize("name", sorted(n for n in INDEX if "reaches_fix" in INDEX[n]))
+def test_fixed_defect_traces_match_the_fixed_oracle(G, name):
+    """Fixtures whose trace reaches a reference defect the product fixes (the
+    oracle's reference mode reproduces the reference build there): from the
+    same boot state, the product gives the fixed oracle's offsets and state."""
+    meta = INDEX[name]
+    boot, _, ops, _, smid = _golden(name)
+    g = G.Gallatin.generate_on_device(meta["arena_bytes"], meta["seed"], boot=False, smid_override=smid)
+    try:
+        g.load(boot)
+        out, _ = g.replay(ops)
+        o = Oracle(meta["arena_bytes"], meta["seed"], fixes=PRODUCT_FIXES, boot=False)
+        o.load(boot)
+        np.testing.assert_array_equal(out, o.replay(ops, smid=smid))
+        assert g.export().diff(o.export()) == []
         assert g.error_word() == 0
     finally:
         g.close()

@@ -85,3 +85,34 @@ def test_a_job_larger_than_the_budget_runs_alone():
     assert admit[1] >= done[0]                       # waited for job 0 to finish
     assert admit[2] >= done[1]                       # and job 2 for the big one
     assert most == 1
+
+
+def test_latency_bins_cover_each_value_within_a_fifth():
+    """Four bins per power of two: every cycle count maps to a bin whose value
+    is within 19% of it, bins grow with the count, and percentiles read from
+    a histogram land on the bin of the true percentile."""
+    from gallatin_gb300.serve import LAT_BINS, bin_value, hist_percentile, lat_bin
+    prev = -1
+    for c in list(range(0, 64)) + [int(1.07 ** k) for k in range(60, 400)]:
+        b = lat_bin(c)
+        assert 0 <= b < LAT_BINS and b >= prev
+        prev = b
+        if c:
+            assert abs(bin_value(b) - c) <= 0.19 * c + 0.5
+    rng = np.random.default_rng(1)
+    x = (2 ** rng.uniform(8, 20, 100_000)).astype(np.int64)
+    h = np.zeros(LAT_BINS, dtype=np.int64)
+    np.add.at(h, [lat_bin(v) for v in x], 1)
+    for q in (50, 99):
+        assert abs(hist_percentile(h, q) - np.percentile(x, q)) <= 0.19 * np.percentile(x, q)
+    assert hist_percentile(np.zeros(LAT_BINS), 50) is None
+
+
+def test_job_grids_and_footprints():
+    """Jobs span one CTA per 2^20 vector elements or 2^18 queue operations
+    (1-8); a multi-CTA vector job reserves the buffers of each CTA's share."""
+    from gallatin_gb300.serve import job_ctas
+    assert job_ctas(JOB_VECTOR, 1000) == 1 and job_ctas(JOB_VECTOR, 3 << 20) == 3
+    assert job_ctas(JOB_VECTOR, 1 << 30) == 8 and job_ctas(JOB_QUEUE, 1 << 20) == 4
+    assert footprint(JOB_VECTOR, 1 << 24) >= 16 * 4 << 20       # 64 MiB of values at least
+    assert footprint(JOB_VECTOR, 1 << 24) <= 4 * 3 * (4 << 20) * 8
