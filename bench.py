@@ -1,12 +1,15 @@
 """Benchmark: malloc+free ops/s on the mixed 16 B–4 KiB churn, one GB300.
 
-Workload (one step): arena 128 GiB (8,192 segments of 16 MiB), 16 rounds of
-4,194,304 device threads each allocating one request (size class uniform over
-32 B..4 KiB, i.e. log-uniform 16 B–4 KiB rounded up to a power of two; request
-sizes non-power-of-two inside the class), a fair coin (Philox4x32-10, seed 1)
-freeing each live allocation before every round but the first, a uint32
-payload written at malloc and checked at free, and a final drain: 64 Mi mallocs
-and 64 Mi frees per step, identical requests every step.
+Workload (one step): an arena of 128 GiB cut into 2,048 segments of 64 MiB
+(Gallatin<64 MiB, 16, 4096>), 16 rounds of 4,194,304 device threads each
+allocating one request (size class uniform over 32 B..4 KiB, i.e. log-uniform
+16 B–4 KiB rounded up to a power of two; request sizes non-power-of-two
+inside the class), a fair coin (Philox4x32-10, seed 1) freeing each live
+allocation before every round but the first, a uint32 payload written at
+malloc and checked at free, and a final drain: 64 Mi mallocs and 64 Mi frees
+per step, identical requests every step.  Both arms run exactly this
+workload and geometry (`config`); the reference arm also reports its own
+default geometry (16 MiB segments).
 
 Arena size: a block of 4,096 slices is reclaimed only when every slice in it
 is freed (the reference's design), and a slice survives k rounds of 50% coin
@@ -17,13 +20,17 @@ failure.  The arena is 128 GiB (2x that) for both arms.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-`value` is the device-resident throughput of the batched path (CTA-aggregated
-persistent kernels, each step one captured CUDA graph); `e2e` is the same churn
-through the public C ABI entry points (gal_malloc_batched / gal_free_batched)
-with each round's request sizes copied from pinned host memory inside the
-timed region.  The plain per-thread path is reported beside it, at the
-reference's knobs (128 pinned slots halving to 4, 16 MiB segments) and at
-the batched form's knobs.
+`value` is the device-resident throughput of the batched path (persistent
+kernels, each step one captured CUDA graph; by default malloc from CTAs that
+cache their SM's pinned blocks in shared memory, frees looking segment
+classes up in a copy staged in shared memory); `e2e` is the same churn through the
+public C ABI entry points (gal_malloc_batched / gal_free_batched_n) with each
+round's request sizes copied from pinned host memory inside the timed region.
+Beside it: every malloc form at the same knobs, on the full churn and on the
+allocator-only churn (no payload), the per-thread path at the reference's
+default knobs, the resident server, per-request latency, and the secondary
+workloads (1 Mi x 16 B stamp, large and block-size allocations, served loop)
+with the reference build's figures where it has the path.
 Multi-GPU: replicas only (each rank its own allocator; no collective on the
 data path); `value` sums all ranks' ops over the slowest rank's time.
 """
@@ -42,13 +49,33 @@ sys.path.insert(0, ROOT)
 
 METRIC = "malloc+free ops/sec, mixed 16B–4KiB, 1 GB300 vs plain/ref; p50/p99 malloc cycles"
 ARENA = 128 << 30
+SEGMENT = 64 << 20
 N_PER_ROUND = 4 << 20
 ROUNDS = 16
 SEED = 1
 ALLOC_SEED = 42
-WORKLOAD = ("mixed-size churn: arena 128 GiB (8192 x 16 MiB segments, Gallatin<16MiB,16,4096>), "
-            "16 rounds x 4,194,304 threads, 50% coin frees before each round, drain; "
-            "uint32 payload written+checked")
+WORKLOAD = ("mixed-size churn: arena 128 GiB as 2,048 segments of 64 MiB (Gallatin<64MiB,16,4096>), "
+            "16 rounds x 4,194,304 threads, sizes log-uniform 16 B-4 KiB, 50% coin frees before each "
+            "round, drain; uint32 payload written+checked")
+# the knobs of this library's throughput settings (gal_config); the reference has none of them
+TUNED = dict(pinned_slots_first=0, pinned_slots_min=0, gather_unlocked_below=16,
+             bytes_per_segment=SEGMENT, spare_blocks=1, block_layout=1)
+# gal_bench_churn modes: bit 0 CTA claim, bit 2 cached pinned blocks, bit 3 allocator-only,
+# bit 7 the cached form at 4 CTAs of 256 threads per SM
+FORMS = {"plain": 0, "cta": 1, "cached": 4}
+SERVER_STREAMS = [          # (requests, lo, hi, log-uniform, kept for this many later requests)
+    (6_000_000, 16, 128, 0, 1),
+    (4_000_000, 16, 4096, 1, 2),
+    (1_000_000, 1024, 32768, 1, 4),
+]
+
+
+def workload_config(n, r, arena):
+    """The workload both arms run (identical dicts)."""
+    return {"workload": WORKLOAD, "arena_bytes": arena, "segment_bytes": SEGMENT, "min_size": 16,
+            "max_size": 4096, "threads_per_round": n, "rounds": r, "seed": SEED,
+            "l2": "no flush needed: the 512 MiB pointer table and the ~56 GB live arena footprint exceed "
+                  "the 129 MB L2"}
 
 
 def parse():
@@ -61,22 +88,18 @@ def parse():
     p.add_argument("--rounds", type=int, default=ROUNDS)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--arena-gib", type=int, default=ARENA >> 30)
-    p.add_argument("--slots", type=int, default=0,
-                   help="pinned slots per size class for the batched form (0: one per SM)")
-    p.add_argument("--unlocked", type=int, default=16,
-                   help="batched form: classes with fewer blocks per segment gather without the lock")
-    p.add_argument("--segment-mib", type=int, default=64, help="batched form: segment size")
-    p.add_argument("--spares", type=int, default=1, choices=[0, 1],
-                   help="batched form: a service warp keeps every pinned slot's next block prepared")
-    p.add_argument("--min-size", type=int, default=16, help="batched form: smallest slice")
-    p.add_argument("--max-size", type=int, default=4096, help="batched form: largest slice")
-    p.add_argument("--free-mode", default="warp", choices=["cta", "warp"],
-                   help="batched form: frees combined per CTA (shared-memory hash) or per warp team")
-    p.add_argument("--quick", action="store_true", help="headline batched steps only (profiling)")
+    p.add_argument("--malloc-form", default="cached", choices=["cached", "cta", "plain"],
+                   help="headline malloc: persistent CTAs with cached pinned blocks, one CTA claim per "
+                        "class, or one thread per request")
+    p.add_argument("--ctas-per-sm", type=int, default=4, choices=[2, 4],
+                   help="cached form: resident CTAs of 256 threads per SM")
+    p.add_argument("--quick", action="store_true", help="headline steps only (profiling)")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the secondary workloads and the reference figures beside them")
     p.add_argument("--configs", action="store_true",
-                   help="instead of the headline: the secondary workloads (tid stamp, serial "
-                        "trace, large and block-size allocations, served loop, hash tables), "
-                        "one JSON line")
+                   help="only the secondary workloads (tid stamp, serial trace, large and block-size "
+                        "allocations, served loop, hash tables), one JSON line")
+    p.add_argument("--only", default="", help="with --configs: comma-separated subset")
     return p.parse_args()
 
 
@@ -198,58 +221,72 @@ def read_profile_traffic(kernel):
     return None
 
 
-def cpu_baseline():
-    """The oracle (the reference allocator's algorithm on one host thread) on a
-    bounded sample of the workload, plus glibc malloc/free on every host core."""
+def cpu_baseline(n=N_PER_ROUND, r=ROUNDS):
+    """The oracle (the reference allocator's algorithm, Gallatin<64 MiB, 16,
+    4096>, on one host thread) on the whole workload, plus glibc malloc/free on
+    every host core on the same requests."""
     import ctypes as C
     from oracle import oracle as orc
     orc.build()
     L = C.CDLL(orc.LIB_PATH)
     L.orc_churn_oracle.restype = C.c_double
-    L.orc_churn_oracle.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p]
+    L.orc_churn_oracle.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p]
     L.orc_churn_glibc.restype = C.c_double
     L.orc_churn_glibc.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_int, C.c_void_p]
     ops = np.zeros(4, dtype=np.uint64)
-    n, r = 1 << 20, 8
-    s = L.orc_churn_oracle(ARENA, n, r, SEED, ops.ctypes.data)
+    s = L.orc_churn_oracle(ARENA, SEGMENT, n, r, SEED, ops.ctypes.data)
     oracle_v = float(ops[0] + ops[2]) / s
     cores = os.cpu_count() or 1
     ops2 = np.zeros(4, dtype=np.uint64)
     s2 = L.orc_churn_glibc(n, r, SEED, cores, ops2.ctypes.data)
     return ({"value": oracle_v, "unit": "ops/s", "cores": 1, "kind": "port",
-             "sample": f"first {r} rounds of the churn at {n} threads/round then drain "
-                       f"({int(ops[0] + ops[2])} ops, {s:.2f} s), the oracle's serial model"},
+             "sample": f"the whole step ({r} rounds x {n} threads then drain, {int(ops[0] + ops[2])} ops, "
+                       f"{s:.2f} s) served by the oracle's serial model of the reference at 64 MiB segments"},
             {"value": float(ops2[0] + ops2[2]) / s2, "unit": "ops/s", "cores": cores,
-             "sample": f"same {r} rounds x {n} requests, glibc malloc/free, payload checked "
+             "sample": f"the same {r} rounds x {n} requests, glibc malloc/free, payload checked "
                        f"({int(ops2[3])} mismatches, {s2:.2f} s)"})
 
 
+# ---------------------------------------------------------------- reference arm
 def run_reference(args, world, rank):
     line = {"impl": "reference", "metric": METRIC, "unit": "ops/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True}
     if rank != 0:
         return None
+    n, r = args.threads_per_round, args.rounds
+    cfg = workload_config(n, r, args.arena_gib << 30)
     try:
         from oracle import refgpu
-        if not refgpu.available():
-            raise FileNotFoundError("reference harness cubin absent")
-        ref = refgpu.RefGPU(ARENA, ALLOC_SEED, refgpu.BOOT_RACY)
+        if not refgpu.available(64) or not refgpu.available(16):
+            raise FileNotFoundError("reference harness cubins absent")
+
+        def churn(seg_mib, steps):
+            ref = refgpu.RefGPU(args.arena_gib << 30, ALLOC_SEED, refgpu.BOOT_RACY, segment_mib=seg_mib)
+            try:
+                return ref.churn(n, r, SEED, args.warmup, steps)
+            finally:
+                ref.close()
+
         with ClockSampler(0) as clk:
-            ms, st = ref.churn(args.threads_per_round, args.rounds, SEED, args.warmup, args.steps)
-        ref.close()
+            ms, st = churn(64, args.steps)
         ops = float(st[0] + st[3])
-        secs = float(ms.sum()) / 1e3
-        v = ops / secs
+        v = ops / (float(ms.sum()) / 1e3)
+        ms16, st16 = churn(16, max(3, args.steps // 4))
+        v16 = float(st16[0] + st16[3]) / (float(ms16.sum()) / 1e3)
         line.update({
             "value": v, "ms_per_step": float(ms.mean()), "scaling": "weak", "vs_baseline": None,
-            "dtype": "u64", "data": "synthetic (Philox4x32-10 seed 1)",
-            "config": {"workload": WORKLOAD, "path": "reference build, plain per-thread malloc/free",
-                       "threads_per_round": args.threads_per_round, "rounds": args.rounds,
-                       "mallocs_failed": int(st[1]), "payload_mismatch": int(st[2]),
-                       "l2": "pointer table 512 MiB > 129 MB L2"},
+            "dtype": "u64", "data": "synthetic (Philox4x32-10 seed 1; sizes log-uniform 16 B-4 KiB rounded to pow2)",
+            "config": cfg,
+            "path": "the reference's own device code (compiled from its sources into oracle/_ref) as "
+                    "Gallatin<64MiB,16,4096>, plain per-thread malloc/free",
+            "mallocs_failed": int(st[1]), "payload_mismatch": int(st[2]),
+            "reference_default_geometry": {
+                "segment_bytes": 16 << 20, "ops_per_s": v16, "ms_per_step": float(ms16.mean()),
+                "mallocs_failed": int(st16[1]), "payload_mismatch": int(st16[2]),
+                "note": "the reference's global type Gallatin<16MiB,16,4096> on the same churn"},
             "cpu_baseline": {"value": v, "unit": "ops/s", "cores": 1, "kind": "reference",
-                             "sample": "whole workload, the reference's own CUDA build (compiled "
-                                       "from its sources into oracle/_ref) on the GPU"},
+                             "sample": "the whole workload, the reference's own CUDA build on the GPU (it has "
+                                       "no CPU implementation of this path)"},
             "e2e": {"value": v, "unit": "ops/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "clocks": clk.summary(),
         })
@@ -257,13 +294,54 @@ def run_reference(args, world, rank):
         base, _ = cpu_baseline()
         line.update({"value": base["value"], "ms_per_step": None, "scaling": "weak",
                      "vs_baseline": None, "dtype": "u64", "data": "synthetic (Philox4x32-10 seed 1)",
-                     "config": {"workload": WORKLOAD, "path": f"oracle port on the CPU ({e})"},
+                     "config": cfg, "path": f"oracle port on the CPU ({e})",
                      "cpu_baseline": base,
                      "e2e": {"value": base["value"], "unit": "ops/s", "h2d_bytes_per_step": 0,
                              "d2h_bytes_per_step": 0}})
     return line
 
 
+def reference_configs(only):
+    """The reference build on the secondary workloads it has a path for: the
+    1 Mi x 16 B tid stamp (its global_test flow) and the large and block-size
+    allocations.  Runs in its own process (driver API)."""
+    from oracle import refgpu
+    out = {"impl": "reference"}
+    if not refgpu.available():
+        out["unavailable"] = "reference build missing (make -C oracle refcubins)"
+        return out
+    if "stamp" in only:
+        ref = refgpu.RefGPU(2 << 30, 42, refgpu.BOOT_RACY)
+        ref.stamp(1 << 20, 16, 1)  # untimed round: first segment gathers
+        rms, rst = ref.stamp(1 << 20, 16, 20)
+        ref.close()
+        out["stamp"] = {"ops_per_s": float(rst[0] + rst[3]) / (float(rms.sum()) / 1e3),
+                        "malloc_ms": float(rms[0]) / 20, "free_ms": float(rms[1]) / 20,
+                        "stamp_errors": int(rst[2]), "failed": int(rst[1]), "rounds": 20}
+    if "large" in only:
+        from gallatin_gb300.workloads import large_block_workload
+        ref = refgpu.RefGPU(64 << 30, 7, refgpu.BOOT_RACY)
+        try:
+            out["large"] = large_block_workload(refgpu.LargeBlockBackend(ref, 7))
+        finally:
+            ref.close()
+    return out
+
+
+def reference_configs_subprocess(only):
+    """reference_configs in a child process; {} when it cannot run."""
+    try:
+        r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--configs", "--impl", "reference",
+                            "--only", ",".join(only)], capture_output=True, text=True, timeout=900)
+        for line in reversed(r.stdout.splitlines()):
+            if line.startswith("{"):
+                return json.loads(line)
+        return {"unavailable": (r.stderr or r.stdout)[-300:]}
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": str(e)[:300]}
+
+
+# ---------------------------------------------------------------- secondary workloads (ours)
 def run_tables(G):
     """512 chained hash tables (2^12-2^22 pairs, seed 3), insert / delete 50% /
     reinsert: batched and per-thread node allocation at the reference's
@@ -300,67 +378,84 @@ def run_tables(G):
     return res
 
 
-def run_configs(impl):
-    """The secondary workloads, one JSON line.  Ours: the 1,048,576 x 16 B tid
-    stamp on 2 GiB (the drop-in per-thread path) and the time of a 4,096-op
-    serial trace replayed by one thread; large and block-size allocations on
-    64 GiB; the served request loop on 32 GiB; 512 chained hash tables with
-    the autotuner.  --impl reference: the same stamp through the reference
-    build (the reference's hash table has no delete and does not compile with
-    nvcc 13, so there is no reference run of the tables)."""
+def ours_stamp(G):
+    """1,048,576 threads x malloc(16) + tid stamp, check, free; 20 rounds on a
+    2 GiB arena at the reference's default knobs (its global_test flow)."""
+    g = G.Gallatin.generate_on_device(2 << 30, 42)
+    try:
+        g.bench_stamp(1 << 20, 16, 1)  # untimed round: module load and first segment gathers
+        ms, st = g.bench_stamp(1 << 20, 16, 20)
+        return {"ops_per_s": float(st[0] + st[3]) / (float(ms.sum()) / 1e3),
+                "malloc_ms": float(ms[0]) / 20, "free_ms": float(ms[1]) / 20,
+                "stamp_errors": int(st[2]), "failed": int(st[1]), "rounds": 20,
+                "error_word": g.error_word()}
+    finally:
+        g.close()
+
+
+def ours_large(G):
+    from gallatin_gb300.workloads import large_block_workload
+    g = G.Gallatin.generate_on_device(64 << 30, 7)
+    try:
+        return large_block_workload(g)
+    finally:
+        g.close()
+
+
+def ours_served(G):
+    from gallatin_gb300 import serve
+    return serve.serve(400, arena_bytes=32 << 30, slots=32)
+
+
+def run_configs(impl, only):
+    """The secondary workloads, one JSON line."""
     import torch
-    n, rounds = 1 << 20, 20
+    only = set(x for x in only.split(",") if x) or {"stamp", "serial", "large", "serve", "tables"}
     out = {"metric": METRIC, "configs": True}
     if impl == "reference":
-        from oracle import refgpu
-        out["impl"] = "reference"
-        if not refgpu.available():
-            out["unavailable"] = "reference build missing (make -C oracle _ref/libref_loader.so)"
-            print(json.dumps(out))
-            return
-        ref = refgpu.RefGPU(2 << 30, 42, refgpu.BOOT_RACY)
-        ref.stamp(n, 16, 1)  # untimed round: first segment gathers
-        rms, rst = ref.stamp(n, 16, rounds)
-        ref.close()
-        out["stamp"] = {"ops_per_s": float(rst[0] + rst[3]) / (float(rms.sum()) / 1e3),
-                        "malloc_ms": float(rms[0]) / rounds, "free_ms": float(rms[1]) / rounds,
-                        "stamp_errors": int(rst[2]), "failed": int(rst[1]), "rounds": rounds}
+        out.update(reference_configs(only))
         print(json.dumps(out))
         return
     import gallatin_gb300 as G
-    from gallatin_gb300 import serve
-    from gallatin_gb300.workloads import large_block_workload, serial_trace
-    g = G.Gallatin.generate_on_device(2 << 30, 42)
-    g.bench_stamp(n, 16, 1)  # untimed round: module load and first segment gathers
-    ms, st = g.bench_stamp(n, 16, rounds)
-    g.close()
-    out["stamp"] = {"ops_per_s": float(st[0] + st[3]) / (float(ms.sum()) / 1e3),
-                    "malloc_ms": float(ms[0]) / rounds, "free_ms": float(ms[1]) / rounds,
-                    "stamp_errors": int(st[2]), "failed": int(st[1]), "rounds": rounds}
-    g = G.Gallatin.generate_on_device(2 << 30, 42)
-    ops_trace = serial_trace(7, 4096)
-    t0 = time.time()
-    offs, _ = g.replay(ops_trace)
-    out["serial_trace"] = {"ops": len(ops_trace), "s": time.time() - t0,
-                           "failed": int((offs[ops_trace < (1 << 63)] == G.FAIL).sum()),
-                           "error_word": g.error_word()}
-    g.close()
-    g = G.Gallatin.generate_on_device(64 << 30, 7)
-    out["large"] = large_block_workload(g)
-    g.close()
-    out["serve"] = serve.serve(400, arena_bytes=32 << 30, slots=32)
-    out["tables"] = run_tables(G)
+    from gallatin_gb300.workloads import serial_trace
+    if "stamp" in only:
+        out["stamp"] = ours_stamp(G)
+    if "serial" in only:
+        g = G.Gallatin.generate_on_device(2 << 30, 42)
+        ops_trace = serial_trace(7, 4096)
+        t0 = time.time()
+        offs, _ = g.replay(ops_trace)
+        out["serial_trace"] = {"ops": len(ops_trace), "s": time.time() - t0,
+                               "failed": int((offs[ops_trace < (1 << 63)] == G.FAIL).sum()),
+                               "error_word": g.error_word()}
+        g.close()
+    if "large" in only:
+        out["large"] = ours_large(G)
+    if "serve" in only:
+        out["serve"] = ours_served(G)
+    if "tables" in only:
+        out["tables"] = run_tables(G)
     torch.cuda.synchronize()
     print(json.dumps(out))
+
+
+# ---------------------------------------------------------------- our arm
+def churn_value(res):
+    return (res.mallocs_ok + res.frees) / (res.ms_total / 1e3)
+
+
+def churn_ok(res):
+    return res.mallocs_failed == 0 and res.payload_mismatch == 0 and res.error_word == 0
 
 
 def main():
     args = parse()
     world, rank, local = dist_setup(args)
     if args.configs:
-        import torch
-        torch.cuda.set_device(local)
-        run_configs(args.impl)
+        if args.impl == "ours":
+            import torch
+            torch.cuda.set_device(local)
+        run_configs(args.impl, args.only)
         return
     if args.impl == "reference":
         line = run_reference(args, world, rank)
@@ -374,27 +469,24 @@ def main():
 
     N, R = args.threads_per_round, args.rounds
     arena = args.arena_gib << 30
-    # the batched form runs with its tuned knobs; the plain per-thread form with
-    # the reference's defaults (128 pinned slots halving to 4)
-    tuned = dict(pinned_slots_first=args.slots, pinned_slots_min=args.slots if args.slots else 0,
-                 gather_unlocked_below=args.unlocked, bytes_per_segment=args.segment_mib << 20,
-                 min_size=args.min_size, max_size=args.max_size, spare_blocks=args.spares)
-    g = G.Gallatin.generate_on_device(arena, ALLOC_SEED, **tuned)
+    occ_bit = 128 if args.ctas_per_sm == 4 else 0
+    form_mode = {"cached": FORMS["cached"] | occ_bit, "cta": FORMS["cta"], "plain": FORMS["plain"]}
+    head_mode = form_mode[args.malloc_form]
+    g = G.Gallatin.generate_on_device(arena, ALLOC_SEED, **TUNED)
 
     # one probe step: a workload that does not fit would run the out-of-memory
     # retry paths for minutes, so stop here instead
-    mode = 1 | (2 if args.free_mode == "cta" else 0)
-    _, probe = g.bench_churn(N, R, SEED, batched=mode, use_graph=False, warmup=0, steps=1)
+    _, probe = g.bench_churn(N, R, SEED, batched=head_mode, use_graph=False, warmup=0, steps=1)
     if probe.mallocs_failed or probe.payload_mismatch or probe.error_word:
         print(json.dumps({"metric": METRIC, "error": "probe step failed", "probe": probe.as_dict()}))
         sys.exit(3)
 
-    # headline: batched + graph
+    # headline: persistent kernels, one CUDA graph per step
     barrier(world)
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         t0 = time.time()
-        ms, res = g.bench_churn(N, R, SEED, batched=mode, use_graph=True,
+        ms, res = g.bench_churn(N, R, SEED, batched=head_mode, use_graph=True,
                                 warmup=args.warmup, steps=args.steps)
         wall = time.time() - t0
     torch.cuda.synchronize()
@@ -422,32 +514,25 @@ def main():
     esecs = max_over_ranks(eres.ms_total / 1e3, world)
     e2e_v = sum_over_ranks(float(eres.mallocs_ok + eres.frees), world) / esecs
     del sizes
+    errors = g.error_word() | eres.error_word
+    if eres.mallocs_failed or eres.payload_mismatch:
+        errors |= 1 << 31
 
-    # p50/p99 per-request latency (clock64 cycles) of one full-concurrency round
-    def lat(a, batched):
-        mc, fc = a.bench_latency(N, SEED + 7, batched)
-        return {"malloc_p50_cycles": float(np.percentile(mc, 50)),
-                "malloc_p99_cycles": float(np.percentile(mc, 99)),
-                "free_p50_cycles": float(np.percentile(fc, 50)),
-                "free_p99_cycles": float(np.percentile(fc, 99))}
-    latency = {"requests": N, "batched": lat(g, True)}
-
-    # roofline of the dominant kernel (malloc or free phase).  HBM: algorithmic
+    # roofline of the dominant kernel of the headline step.  HBM: algorithmic
     # bytes per launch -- malloc: 8 B pointer store + 4 B payload store per
-    # request; free: 8 B pointer load per slot scanned (rounds 1..R-1 scan
-    # r*N slots, the drain R*N) + 4 B payload load + 8 B pointer clear per
-    # free; allocator metadata stays in L2.  L2 atomics: one counter atomic
-    # per request (the per-block malloc or free counter) against the measured
-    # atomic peak.
+    # request; free: 8 B pointer load + 4 B payload load + 8 B pointer clear
+    # per free, plus 4 B of liveness word per 32 slots scanned.  L2 atomics:
+    # one counter atomic per request (the per-block malloc or free counter)
+    # against the atomic peak measured in this run.
     distinct, same = G.atomic_peak()
-    per_step_mallocs = res.mallocs_ok / args.steps
     hbm_peak, peak_src = measured_hbm_peak()
-    free_kern = "k_churn_free_batched" if args.free_mode == "cta" else "k_churn_free_plain"
+    malloc_kern = {"cached": "k_churn_malloc_cached", "cta": "k_churn_malloc_batched",
+                   "plain": "k_churn_malloc_plain"}[args.malloc_form]
+    free_kern = "k_churn_free_plain"
+    scanned = N * R * (R + 1) / 2 * args.steps
     phases = {
-        "k_churn_malloc_batched": (res.ms_malloc_kernels, res.malloc_launches, res.mallocs_ok,
-                                   12.0 * res.mallocs_ok),
-        free_kern: (res.ms_free_kernels, res.free_launches, res.frees,
-                    8.0 * N * R * (R + 1) / 2 * args.steps + 12.0 * res.frees),
+        malloc_kern: (res.ms_malloc_kernels, res.malloc_launches, res.mallocs_ok, 12.0 * res.mallocs_ok),
+        free_kern: (res.ms_free_kernels, res.free_launches, res.frees, scanned / 8 + 20.0 * res.frees),
     }
 
     def roofline_of(kern):
@@ -473,33 +558,87 @@ def main():
                                              "distinct addresses in a 32 MiB L2-resident buffer",
                               "same_address_peak": same / 1e9}}
 
-    dominant = ("k_churn_malloc_batched" if res.ms_malloc_kernels >= res.ms_free_kernels
-                else free_kern)
+    dominant = malloc_kern if res.ms_malloc_kernels >= res.ms_free_kernels else free_kern
     roofline = roofline_of(dominant)
     roofline["other_phase"] = {k: v for k, v in roofline_of(
-        free_kern if dominant == "k_churn_malloc_batched" else "k_churn_malloc_batched").items()
-        if k not in ("peak_source",)}
-    errors = g.error_word()
+        free_kern if dominant == malloc_kern else malloc_kern).items() if k not in ("peak_source",)}
+
+    # p50/p99 per-request latency (clock64 cycles) of one full-concurrency round
+    def lat(a, batched):
+        mc, fc = a.bench_latency(N, SEED + 7, batched)
+        return {"malloc_p50_cycles": float(np.percentile(mc, 50)),
+                "malloc_p99_cycles": float(np.percentile(mc, 99)),
+                "free_p50_cycles": float(np.percentile(fc, 50)),
+                "free_p99_cycles": float(np.percentile(fc, 99))}
+    latency = {"requests": N, "cached": lat(g, 2), "cta_claim": lat(g, 1), "plain_tuned_knobs": lat(g, 0)}
     g.close()
 
-    # plain per-thread path on the reference's default knobs, stream launches
+    # every malloc form at the same knobs, full churn and allocator-only churn
+    steps_f = max(3, args.steps // 3)
+    forms = {}
+    for name, mode in (("plain", 0), ("cta", FORMS["cta"]), ("cached", FORMS["cached"] | occ_bit)):
+        entry = {}
+        for bare, key in ((0, "full"), (8, "allocator_only")):
+            gf = G.Gallatin.generate_on_device(arena, ALLOC_SEED, **TUNED)
+            try:
+                _, rf = gf.bench_churn(N, R, SEED, batched=mode | bare, use_graph=True, warmup=1, steps=steps_f)
+                errors |= rf.error_word | (0 if churn_ok(rf) else 1 << 31)
+            finally:
+                gf.close()
+            v = churn_value(rf)
+            step_ms = rf.ms_total / steps_f
+            mall = rf.mallocs_ok / steps_f
+            e = {"ops_per_s": v, "ms_per_step": step_ms, "malloc_kernels_ms": rf.ms_malloc_kernels / steps_f,
+                 "free_kernels_ms": rf.ms_free_kernels / steps_f}
+            # one claim atomic per malloc and one free-counter atomic per free,
+            # over each phase's kernel time, against the in-run atomic peak
+            e["malloc_l2_atomic_frac"] = mall / (rf.ms_malloc_kernels / steps_f / 1e3) / distinct
+            e["free_l2_atomic_frac"] = (rf.frees / steps_f) / (rf.ms_free_kernels / steps_f / 1e3) / distinct
+            entry[key] = e
+        forms[name] = entry
+    forms["note"] = ("same knobs for every form: one pinned slot per SM, 64 MiB segments, lock-free gathers "
+                     "below 16 blocks per segment, spare blocks, one 32-byte record per block; "
+                     "allocator_only = the same requests, frees and pointer stores without the payload "
+                     "word; l2_atomic_frac = one counter atomic per request over the phase's kernel time "
+                     "against the in-run atomicAdd peak")
+
+    # the per-thread path at the reference's default knobs (128 pinned slots
+    # halving to 4, 16 MiB segments, no spare blocks)
     gp = G.Gallatin.generate_on_device(arena, ALLOC_SEED)
-    plain_ms, plain = gp.bench_churn(N, R, SEED, batched=False, use_graph=False,
-                                     warmup=1, steps=max(1, args.steps // 2))
-    plain_v = (plain.mallocs_ok + plain.frees) / (plain.ms_total / 1e3)
-    latency["plain"] = lat(gp, False)
+    _, plain = gp.bench_churn(N, R, SEED, batched=False, use_graph=False, warmup=1, steps=max(1, args.steps // 3))
+    plain_v = churn_value(plain)
+    latency["plain_default_knobs"] = lat(gp, 0)
     errors |= gp.error_word()
     gp.close()
-    # the same per-thread calls on the batched form's knobs
-    gt = G.Gallatin.generate_on_device(arena, ALLOC_SEED, **tuned)
-    _, plain_t = gt.bench_churn(N, R, SEED, batched=False, use_graph=True,
-                                warmup=1, steps=max(1, args.steps // 2))
-    plain_tuned_v = (plain_t.mallocs_ok + plain_t.frees) / (plain_t.ms_total / 1e3)
-    latency["plain_tuned_knobs"] = lat(gt, False)
-    errors |= gt.error_word() | plain_t.error_word
-    if plain_t.mallocs_failed or plain_t.payload_mismatch:
-        errors |= 1 << 31
-    gt.close()
+
+    # the resident server against the same producers calling malloc directly
+    server = {}
+    if world == 1:
+        for key, direct in (("server", False), ("direct", True)):
+            gs = G.Gallatin.generate_on_device(32 << 30, ALLOC_SEED, **TUNED)
+            try:
+                sms, sr = gs.bench_server(SERVER_STREAMS, server_pct=25, direct=direct, use_graph=True,
+                                          warmup=1, steps=3)
+            finally:
+                gs.close()
+            server[key] = {"ops_per_s": (sr.mallocs_ok + sr.frees) / (sr.ms_total / 1e3),
+                           "ms_per_step": sr.ms_total / 3, "violations": int(sr.stamp_mismatch + sr.misaligned),
+                           "failed": int(sr.mallocs_failed), "status": int(sr.status),
+                           "grid": int(sr.grid), "server_ctas": int(sr.server_ctas), "graph": bool(sr.graph)}
+        server["streams"] = [list(s) for s in SERVER_STREAMS]
+
+    # secondary workloads, ours and the reference build's
+    configs = {}
+    if world == 1 and not args.no_extras:
+        configs["1_stamp"] = {"ours": ours_stamp(G)}
+        configs["3_large"] = {"ours": ours_large(G)}
+        served = ours_served(G)
+        configs["5_served"] = {"ours": {k: served[k] for k in served if k != "checksums"}}
+        ref = reference_configs_subprocess(["stamp", "large"])
+        configs["1_stamp"]["reference"] = ref.get("stamp", ref.get("unavailable"))
+        configs["3_large"]["reference"] = ref.get("large", ref.get("unavailable"))
+        configs["5_served"]["reference"] = ("n/a: the reference's queue (data_structs/queue.cuh) does not "
+                                            "compile with nvcc 13")
 
     if rank != 0:
         return
@@ -508,20 +647,23 @@ def main():
         "warmup": args.warmup, "ms_per_step": secs * 1e3 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic (Philox4x32-10 seed 1; sizes log-uniform 16 B-4 KiB rounded to pow2)",
-        "config": {"workload": WORKLOAD, "path": "batched: CTA-aggregated persistent kernels, one CUDA graph per step",
-                   "pinned_slots_batched": args.slots or "one per SM", "pinned_slots_plain": "128 halving to 4 (default config: 16 MiB segments, lock-free gathers below 16 blocks per segment, no spare blocks)",
-                   "batched_knobs": {"gather_unlocked_below": args.unlocked, "segment_mib": args.segment_mib,
-                                     "spare_blocks": args.spares,
-                                     "min_size": args.min_size, "max_size": args.max_size,
-                                     "free_mode": args.free_mode},
-                   "arena_bytes": arena, "threads_per_round": N, "rounds": R,
-                   "l2": "no flush needed: the 512 MiB pointer table and the ~56 GB live arena footprint exceed the 129 MB L2",
-                   "plain_ops_per_s": plain_v, "batched_over_plain": value / plain_v / world,
-                   "plain_tuned_knobs_ops_per_s": plain_tuned_v,
-                   "batched_over_plain_tuned_knobs": value / plain_tuned_v / world,
-                   "mallocs_per_step": per_step_mallocs, "mallocs_failed": res.mallocs_failed,
-                   "payload_mismatch": res.payload_mismatch, "device_error_word": errors,
-                   "wall_s_timed": wall},
+        "config": workload_config(N, R, arena),
+        "path": {"cached": "persistent malloc CTAs (%d x 256 threads per SM) that keep their SM's pinned "
+                           "blocks in shared memory, one atomicAdd per warp team; persistent free phase "
+                           "with segment classes staged in shared memory, one atomic per warp team; "
+                           "one CUDA graph per step" % args.ctas_per_sm,
+                 "cta": "persistent kernels, one CTA claim per class, frees in warp teams, one CUDA graph "
+                        "per step",
+                 "plain": "one thread per request, frees in warp teams, one CUDA graph per step"}[args.malloc_form],
+        "knobs": dict(TUNED, note="gal_config fields; pinned_slots_first=0 means one pinned slot per SM "
+                                  "in every class"),
+        "mallocs_per_step": res.mallocs_ok / args.steps, "mallocs_failed": int(res.mallocs_failed),
+        "payload_mismatch": int(res.payload_mismatch), "device_error_word": int(errors | res.error_word),
+        "wall_s_timed": wall,
+        "plain_default_knobs_ops_per_s": plain_v,
+        "batched_over_plain_default_knobs": value / plain_v / world,
+        "batched_over_plain_same_knobs": value / forms["plain"]["full"]["ops_per_s"] / world,
+        "forms_same_knobs": forms,
         "roofline": roofline,
         "e2e": {"value": e2e_v, "unit": "ops/s", "h2d_bytes_per_step": int(eres.h2d_bytes),
                 "d2h_bytes_per_step": int(eres.d2h_bytes),
@@ -531,11 +673,13 @@ def main():
                         "round's allocator calls on its own stream; the step captured once as a "
                         "CUDA graph (three streams)"},
         "latency": latency,
+        "server": server,
+        "configs_secondary": configs,
         "gpu_launches": int(res.malloc_launches + res.free_launches),
         "clocks": clk.summary(),
     }
     if world == 1 and not args.no_cpu_baseline:
-        base, glibc = cpu_baseline()
+        base, glibc = cpu_baseline(N, R)
         line["cpu_baseline"] = base
         line["host_malloc_baseline"] = glibc
     print(json.dumps(line))

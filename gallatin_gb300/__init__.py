@@ -50,6 +50,38 @@ class ChurnResult(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class ServerStream(C.Structure):
+    """gal_server_stream (gallatin_gb300/csrc/gal_server.cu)."""
+    _fields_ = [
+        ("requests", C.c_uint64),
+        ("lo", C.c_uint32),
+        ("hi", C.c_uint32),
+        ("log_uniform", C.c_uint32),
+        ("keep", C.c_uint32),
+    ]
+
+
+class ServerResult(C.Structure):
+    """gal_server_result (gallatin_gb300/csrc/gal_server.cu)."""
+    _fields_ = [
+        ("ms_total", C.c_double),
+        ("mallocs_ok", C.c_uint64),
+        ("mallocs_failed", C.c_uint64),
+        ("stamp_mismatch", C.c_uint64),
+        ("frees", C.c_uint64),
+        ("misaligned", C.c_uint64),
+        ("status", C.c_uint32),
+        ("error_word", C.c_uint32),
+        ("grid", C.c_uint32),
+        ("server_ctas", C.c_uint32),
+        ("block", C.c_uint32),
+        ("graph", C.c_int),
+    ]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 class TablesResult(C.Structure):
     """gal_tables_result (gallatin_gb300/csrc/gal_tables.cu)."""
     _fields_ = [
@@ -124,6 +156,7 @@ def lib():
         "gal_bench_latency": ([vp, u64, u32, C.c_int, vp, vp], C.c_int),
         "gal_bench_atomic_peak": ([vp, vp], C.c_int),
         "gal_bench_sector_probe": ([u32, u32, vp], C.c_int),
+        "gal_bench_server": ([vp, vp, u32, u32, C.c_int, C.c_int, C.c_int, C.c_int, u32, vp, vp], C.c_int),
         "gal_job_launch": ([vp, u32, u64, u64, vp, vp, vp], C.c_int),
         "gal_job_ctas": ([u32, u64], u32),
         "gal_bench_tables": ([vp, u32, vp, u64, C.c_int, vp, u32, vp, vp, u64, vp], C.c_int),
@@ -357,6 +390,18 @@ class Gallatin:
                                       n.ctypes.data if dump else None), "gal_bench_tables")
         got = int(min(n[0], dump_cap)) if dump else 0
         return r, keys[:got], vals[:got]
+
+    def bench_server(self, streams, server_pct=25, direct=False, use_graph=True, warmup=1, steps=3,
+                     deadline_ms=5000):
+        """The resident-server workload (gal_server.cu): streams are
+        (requests, lo, hi, log_uniform, keep) tuples.  Returns (step ms, ServerResult)."""
+        arr = (ServerStream * len(streams))(*[ServerStream(*x) for x in streams])
+        ms = np.zeros(max(steps, 1), dtype=np.float32)
+        r = ServerResult()
+        _check(lib().gal_bench_server(self._h, arr, len(streams), server_pct, int(direct), int(use_graph),
+                                      warmup, steps, deadline_ms, ms.ctypes.data, C.byref(r)),
+               "gal_bench_server")
+        return ms[:steps], r
 
     def bench_stamp(self, n, size, rounds=1):
         ms = np.zeros(2, dtype=np.float32)

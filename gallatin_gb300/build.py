@@ -15,7 +15,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgallatin_gb300.so")
-SOURCES = ["gal_lib.cu", "gal_bench.cu", "gal_noalloc.cu", "gal_serve.cu", "gal_tables.cu"]
+SOURCES = ["gal_lib.cu", "gal_bench.cu", "gal_noalloc.cu", "gal_serve.cu", "gal_tables.cu", "gal_server.cu"]
 HEADERS = [
     os.path.join(ROOT, "include", "gallatin_gb300.h"),
     os.path.join(ROOT, "include", "gallatin_gb300", "gal_device.cuh"),
@@ -23,6 +23,7 @@ HEADERS = [
     os.path.join(CSRC, "churn.cuh"),
     os.path.join(CSRC, "workload.cuh"),
     os.path.join(CSRC, "gal_internal.h"),
+    os.path.join(CSRC, "gal_server.cuh"),
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include")]

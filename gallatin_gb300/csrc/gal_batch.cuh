@@ -218,56 +218,30 @@ __device__ __forceinline__ void *cta_malloc(const state *s, uint64_t size, bool 
   return out[0];
 }
 
-// ------------------------------------------------------------ CTA reservoirs
-// Each CTA keeps, per size class, one run of slices reserved from its SM's
-// pinned block in shared memory, packed in one 64-bit word:
-//   bits 63-32 block id, bits 31-13 cursor (next slice), bits 12-0 end.
-// A warp team of k lanes asking for class t adds k to the cursor with one
-// shared-memory atomic and takes slices [cursor, cursor + k) while they lie
-// below the end.  The one team whose interval holds the end (the crosser)
-// takes what is left, reserves the next run from the pinned block with one
-// global atomicAdd of the run length (replacing the block when the run
-// crosses slice 4095, exactly as a per-thread team does) and publishes it;
-// teams that arrive while a run is exhausted and not yet replaced claim their
-// slices from the pinned block directly (the per-thread path), so no warp
-// ever waits on another.  At the end the CTA credits the slices left in its
-// runs as freed, so their blocks still return once everything else in them
-// is freed.  Global atomics: one per run instead of one per warp team.
-static constexpr uint32_t RES_END_BITS = 13;
-static constexpr uint32_t RES_CURSOR_LIMIT = 1u << 18;  // cursor field has 19 bits
-
-struct cta_res_smem {
-  unsigned long long desc[GAL_MAX_TREES];
-  uint32_t slot[GAL_MAX_TREES];  // pinned slot the class's runs came from
-  uint32_t blk[GAL_MAX_TREES];   // the block of that slot last drawn from (NOBLK: read the slot)
-  uint32_t run;                  // slices per run
+// ------------------------------------------------------------ runs of slices
+// The pinned block a CTA last claimed a run from, per class (claim_run).
+struct run_cache {
+  uint32_t blk[GAL_MAX_TREES];  // NOBLK: read the pinned slot
+  uint32_t slot[GAL_MAX_TREES];
 };
 
-GAL_DEVICE_INLINE unsigned long long res_desc(uint32_t blk, uint32_t cursor, uint32_t end) {
-  return ((unsigned long long)blk << 32) | ((unsigned long long)cursor << RES_END_BITS) | end;
-}
-
-// Call once by every thread of the CTA before the first res_malloc, followed
-// by a __syncthreads().  run: slices reserved per refill (1..4096).
-__device__ __forceinline__ void cta_res_init(cta_res_smem &sm, uint32_t run) {
+GAL_DEVICE_INLINE void run_cache_init(run_cache &c) {
   if (threadIdx.x < GAL_MAX_TREES) {
-    sm.desc[threadIdx.x] = res_desc(NOBLK, 0, 0);  // empty: the first team crosses
-    sm.slot[threadIdx.x] = 0;
-    sm.blk[threadIdx.x] = NOBLK;
+    c.blk[threadIdx.x] = NOBLK;
+    c.slot[threadIdx.x] = 0;
   }
-  if (threadIdx.x == 0) sm.run = run < 1 ? 1 : run > SLICES_PER_BLOCK ? SLICES_PER_BLOCK : run;
 }
 
-// Reserves the next run of class `tree` from the pinned block (one lane).
-// Returns the run's descriptor, or an empty one when no block could be had.
-// When the run crossed the end of its block and a spare block was swapped in,
-// spare_slot receives the slot whose spare the caller should prepare again
-// (after publishing the run), else NOBLK.
-GAL_DEVICE_COLD unsigned long long res_refill(const state *s, uint32_t tree, cta_res_smem &sm,
-                                              uint32_t &spare_slot) {
+// One thread claims a run of up to `want` slices of class `tree` with one
+// atomicAdd on the pinned block (the block of the CTA's last run while it
+// lasts).  Returns the run's length (0: no block to be had), its block and
+// first slice.  When the run crossed the end of its block and a spare block
+// was swapped in, spare_slot receives the slot whose spare the caller should
+// prepare again (after using the run), else NOBLK.
+GAL_DEVICE_COLD uint32_t claim_run(const state *s, uint32_t tree, uint32_t want, run_cache &rc, uint32_t &run_blk,
+                                   uint32_t &run_start, uint32_t &spare_slot) {
   const uint64_t tid = thread_linear_id();
-  const uint32_t want = sm.run;
-  uint32_t blk = sm.blk[tree], slot = sm.slot[tree];
+  uint32_t blk = rc.blk[tree], slot = rc.slot[tree];
   spare_slot = NOBLK;
   for (int attempt = 0; attempt < CTA_CLAIM_ATTEMPTS; attempt++) {
     if (blk == NOBLK) {
@@ -297,91 +271,16 @@ GAL_DEVICE_COLD unsigned long long res_refill(const state *s, uint32_t tree, cta
       }
       blk = NOBLK;
     }
-    sm.blk[tree] = blk;
-    sm.slot[tree] = slot;
-    if (mine) return res_desc(used, (uint32_t)cnt, (uint32_t)(cnt + got));
-  }
-  sm.blk[tree] = NOBLK;
-  return res_desc(NOBLK, 0, 0);
-}
-
-// malloc through the CTA's reservoirs: single slices of a class draw from the
-// class's run; everything else (runs of slices, blocks, segment runs,
-// exhausted reservoirs) takes the per-thread path.  Called by any subset of
-// the CTA's lanes, like gal::malloc; every warp-wide step names the lanes
-// that entered together, which all run the same number of passes.
-__device__ __forceinline__ void *res_malloc(const state *s, uint64_t size, cta_res_smem &sm) {
-  const int T = (int)s->num_trees;
-  const int bits = ceil_log2(size);
-  const int t = (size >> s->min_shift) == 0 ? 0 : bits - (int)s->min_shift;
-  const uint32_t callers = active_lanes();
-  const uint32_t lane = lane_id();
-  bool want = t < T;  // still asking the reservoir for a slice
-  void *p = nullptr;
-  for (int pass = 0; pass < 3; pass++) {
-    if (__ballot_sync(callers, want) == 0) break;
-    const uint32_t team = __match_any_sync(callers, want ? t : -1);
-    const int leader = __ffs(team) - 1;
-    const uint32_t k = (uint32_t)__popc(team);
-    const uint32_t rank = (uint32_t)__popc(team & lanemask_lt());
-    unsigned long long d = 0;
-    int go = 0;
-    if (want && (int)lane == leader) {
-      const unsigned long long seen = *(volatile unsigned long long *)&sm.desc[t];
-      const uint32_t c0 = (uint32_t)(seen >> RES_END_BITS) & (2 * RES_CURSOR_LIMIT - 1);
-      // an exhausted run is not added to, which keeps the cursor field small
-      go = c0 <= (uint32_t)(seen & ((1u << RES_END_BITS) - 1)) && c0 < RES_CURSOR_LIMIT;
-      d = go ? atomicAdd(&sm.desc[t], (unsigned long long)k << RES_END_BITS) : seen;
+    rc.blk[tree] = blk;
+    rc.slot[tree] = slot;
+    if (mine) {
+      run_blk = used;
+      run_start = (uint32_t)cnt;
+      return got;
     }
-    go = __shfl_sync(callers, go, leader);
-    d = __shfl_sync(callers, d, leader);
-    bool crosser = false;
-    if (want) {
-      const uint32_t blk = (uint32_t)(d >> 32);
-      const uint32_t c = (uint32_t)(d >> RES_END_BITS) & (2 * RES_CURSOR_LIMIT - 1);
-      const uint32_t e = (uint32_t)(d & ((1u << RES_END_BITS) - 1));
-      if (!go) {
-        want = false;  // exhausted and being replaced by another team: claim directly
-      } else {
-        crosser = c <= e && e < c + k;
-        if (blk != NOBLK && c + rank < e) {
-          p = slice_ptr(s, blk, c + rank, (uint32_t)t);
-          want = false;
-        } else if (!crosser) {
-          want = false;  // beyond the end of a run another team replaces
-        }
-      }
-    }
-    // the crosser's leader reserves and publishes the next run; the crosser's
-    // lanes still without a slice take theirs from it on the next pass
-    unsigned long long nd = 0;
-    if (crosser && (int)lane == leader) {
-      uint32_t spare_slot;
-      nd = res_refill(s, (uint32_t)t, sm, spare_slot);
-      atomicExch(&sm.desc[t], nd);
-      if (spare_slot != NOBLK) refill_spare(s, (uint32_t)t, spare_slot, thread_linear_id());
-    }
-    nd = __shfl_sync(callers, nd, leader);
-    if (crosser && want && (uint32_t)(nd >> 32) == NOBLK) want = false;
   }
-  if (p) {
-    if (s->zero_fill) zero_fill(p, size);
-    return p;
-  }
-  return malloc_fallback(s, size);  // clears its own bytes in calloc mode
-}
-
-// Call by every thread of the CTA after its last res_malloc, after a
-// __syncthreads(): the slices left in the CTA's runs are credited as freed.
-__device__ __forceinline__ void cta_res_release(const state *s, cta_res_smem &sm) {
-  if (threadIdx.x < (uint32_t)s->num_trees) {
-    const unsigned long long d = sm.desc[threadIdx.x];
-    const uint32_t blk = (uint32_t)(d >> 32);
-    const uint32_t c = (uint32_t)(d >> RES_END_BITS) & (RES_CURSOR_LIMIT * 2 - 1);
-    const uint32_t e = (uint32_t)(d & ((1u << RES_END_BITS) - 1));
-    if (blk != NOBLK && c < e) credit_frees(s, blk, e - c);
-    sm.desc[threadIdx.x] = res_desc(NOBLK, 0, 0);
-  }
+  rc.blk[tree] = NOBLK;
+  return 0;
 }
 
 template <int SLOTS>

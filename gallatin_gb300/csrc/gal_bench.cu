@@ -35,6 +35,7 @@ namespace {
 
 struct plain_alloc {
   const gal::state *s;
+  const uint16_t *classes;  // staged segment classes (gal::stage_classes) or nullptr
   __device__ void *malloc(uint64_t n) { return gal::malloc(s, n); }
   __device__ void free(void *p) { gal::free(s, p); }
 };
@@ -46,7 +47,7 @@ template <>
 struct galwl::free_many<plain_alloc> {
   static __device__ __forceinline__ void run(plain_alloc *a, void *const (&p)[galwl::FREE_SLOTS],
                                              const bool (&go)[galwl::FREE_SLOTS]) {
-    gal::free_n<galwl::FREE_SLOTS>(a->s, p, go);
+    gal::free_n<galwl::FREE_SLOTS>(a->s, p, go, a->classes);
   }
 };
 
@@ -57,46 +58,51 @@ constexpr int BT = 512;  // batched CTA size
 template <bool PAYLOAD>
 __global__ void k_churn_malloc_plain(const gal::state *s, void **ptrs, uint32_t *live, uint64_t base,
                                      uint64_t n, uint32_t seed, unsigned long long *stats) {
-  plain_alloc a{s};
+  plain_alloc a{s, nullptr};
   galwl::churn_malloc_body<plain_alloc, PAYLOAD>(&a, ptrs, live, base, n, seed, stats);
 }
 
 constexpr int FREE_BT = 256;  // free phase CTA size (persistent grid)
 
+// The free phase; with dynamic shared memory of 2 bytes per segment the
+// segments' classes are staged first (every pointer freed here was allocated
+// by an earlier kernel, and a live pointer's segment keeps its class).
 template <bool PAYLOAD>
 __global__ void __launch_bounds__(FREE_BT)
     k_churn_free_plain(const gal::state *s, void **ptrs, uint32_t *live, uint64_t nslots,
-                       uint32_t round, uint32_t seed, int all, unsigned long long *stats) {
+                       uint32_t round, uint32_t seed, int all, int stage, unsigned long long *stats) {
   __shared__ uint16_t lists[FREE_BT / 32][galwl::WARP_SLOTS];
-  plain_alloc a{s};
+  extern __shared__ uint16_t classes[];
+  const bool staged = stage && gal::stage_classes(s, classes);
+  __syncthreads();
+  plain_alloc a{s, staged ? classes : nullptr};
   galwl::churn_free_warps<plain_alloc, PAYLOAD>(&a, ptrs, live, nslots, round, seed, all != 0, stats,
                                                 lists[threadIdx.x >> 5]);
 }
 
-// persistent malloc phase of one round through the CTA reservoirs
-// (gal::res_malloc): each thread serves slots c + threadIdx.x of the CTA's
-// chunks, so a warp's lanes keep 32 consecutive slots for the liveness words
-constexpr int RES_BT = 256;
-template <bool PAYLOAD>
-__global__ void __launch_bounds__(RES_BT)
-    k_churn_malloc_res(const gal::state *s, void **ptrs, uint32_t *live, uint64_t base, uint64_t n,
-                       uint32_t seed, uint32_t run, unsigned long long *stats) {
-  __shared__ gal::cta_res_smem sm;
-  gal::cta_res_init(sm, run);
+// persistent malloc phase of one round with the pinned blocks cached per CTA
+// (gal::malloc_cached): each thread serves slots c + threadIdx.x of the CTA's
+// chunks, so a warp's lanes keep 32 consecutive slots for the liveness words.
+// MINB: CTAs per SM the registers must allow (64 registers at 4).
+constexpr int CACHED_BT = 256;
+template <bool PAYLOAD, int MINB>
+__global__ void __launch_bounds__(CACHED_BT, MINB)
+    k_churn_malloc_cached(const gal::state *s, void **ptrs, uint32_t *live, uint64_t base, uint64_t n,
+                          uint32_t seed, unsigned long long *stats) {
+  __shared__ gal::slot_cache cache;
+  gal::slot_cache_init(cache);
   __syncthreads();
-  for (uint64_t c = (uint64_t)blockIdx.x * RES_BT; c < n; c += (uint64_t)gridDim.x * RES_BT) {
+  for (uint64_t c = (uint64_t)blockIdx.x * CACHED_BT; c < n; c += (uint64_t)gridDim.x * CACHED_BT) {
     const uint64_t t = c + threadIdx.x;
     if (t >= n) break;  // whole warps: n is a multiple of SLOT_ALIGN
     const uint64_t slot = base + t;
-    void *p = gal::res_malloc(s, galwl::mixed_size(slot, seed), sm);
+    void *p = gal::malloc_cached(s, galwl::mixed_size(slot, seed), cache);
     if (PAYLOAD && p) *(volatile uint32_t *)p = galwl::payload(slot, seed);
     ptrs[slot] = p;
     galwl::publish_live(live, slot, p != nullptr);
     galwl::warp_count(&stats[0], p != nullptr);
     galwl::warp_count(&stats[1], p == nullptr);
   }
-  __syncthreads();
-  gal::cta_res_release(s, sm);
 }
 
 // persistent, CTA-aggregated malloc phase of one round: BW worker threads and
@@ -276,25 +282,23 @@ __global__ void __launch_bounds__(BT)
   gal::cta_workers_done(sm);
 }
 
-__global__ void __launch_bounds__(RES_BT)
-    k_lat_malloc_res(const gal::state *s, void **ptrs, uint64_t base, uint64_t n, uint32_t seed,
-                     uint32_t *cycles) {
-  __shared__ gal::cta_res_smem sm;
-  gal::cta_res_init(sm, 128);
+__global__ void __launch_bounds__(CACHED_BT)
+    k_lat_malloc_cached(const gal::state *s, void **ptrs, uint64_t base, uint64_t n, uint32_t seed,
+                        uint32_t *cycles) {
+  __shared__ gal::slot_cache cache;
+  gal::slot_cache_init(cache);
   __syncthreads();
-  for (uint64_t c = (uint64_t)blockIdx.x * RES_BT; c < n; c += (uint64_t)gridDim.x * RES_BT) {
+  for (uint64_t c = (uint64_t)blockIdx.x * CACHED_BT; c < n; c += (uint64_t)gridDim.x * CACHED_BT) {
     const uint64_t t = c + threadIdx.x;
     if (t >= n) break;
     const uint64_t size = galwl::mixed_size(base + t, seed);
     long long c0 = clock64();
-    void *p = gal::res_malloc(s, size, sm);
+    void *p = gal::malloc_cached(s, size, cache);
     long long c1 = clock64();
     if (p) *(volatile uint32_t *)p = galwl::payload(base + t, seed);
     ptrs[base + t] = p;
     cycles[t] = (uint32_t)min(c1 - c0, 0xFFFFFFFFll);
   }
-  __syncthreads();
-  gal::cta_res_release(s, sm);
 }
 
 // the batched free path (gal_free_batched): warp teams per block through
@@ -353,8 +357,9 @@ struct churn_ctx {
   uint32_t R, seed;
   int batched;
   bool payload;   // false: the allocator-only form (no payload written or checked)
-  uint32_t run;   // reservoir run length (slices)
-  int grid_r;     // persistent grid of the reservoir malloc
+  int minb;       // cached malloc: CTAs per SM its registers allow (2 or 4)
+  int grid_c;     // persistent grid of the cached malloc
+  size_t stage_bytes;  // dynamic shared memory of the free phase: staged segment classes (0: none)
   void **ptrs;
   uint32_t *live;  // slot liveness bits (churn.cuh)
   unsigned long long *stats;
@@ -394,11 +399,11 @@ void enqueue_step(churn_ctx &c, cudaStream_t st, bool capturing) {
         const uint64_t chunk = (uint64_t)(FREE_BT / 32) * galwl::WARP_SLOTS;
         unsigned g = (unsigned)std::min<uint64_t>((nscan + chunk - 1) / chunk, (uint64_t)c.grid_f);
         if (c.payload)
-          k_churn_free_plain<true><<<g, FREE_BT, 0, st>>>(c.d, c.ptrs, c.live, nscan, r, c.seed,
-                                                         drain ? 1 : 0, c.stats);
+          k_churn_free_plain<true><<<g, FREE_BT, c.stage_bytes, st>>>(c.d, c.ptrs, c.live, nscan, r, c.seed,
+                                                                     drain ? 1 : 0, c.stage_bytes > 0, c.stats);
         else
-          k_churn_free_plain<false><<<g, FREE_BT, 0, st>>>(c.d, c.ptrs, c.live, nscan, r, c.seed,
-                                                          drain ? 1 : 0, c.stats);
+          k_churn_free_plain<false><<<g, FREE_BT, c.stage_bytes, st>>>(c.d, c.ptrs, c.live, nscan, r, c.seed,
+                                                                      drain ? 1 : 0, c.stage_bytes > 0, c.stats);
       }
       mark(1, false);
     }
@@ -406,13 +411,18 @@ void enqueue_step(churn_ctx &c, cudaStream_t st, bool capturing) {
     uint64_t base = c.N * r;
     mark(0, true);
     if (c.batched & 4) {
-      const unsigned gr = (unsigned)std::min<uint64_t>((c.N + RES_BT - 1) / RES_BT, (uint64_t)c.grid_r);
-      if (c.payload)
-        k_churn_malloc_res<true><<<gr, RES_BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.run,
-                                                       c.stats);
-      else
-        k_churn_malloc_res<false><<<gr, RES_BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.run,
-                                                        c.stats);
+      const unsigned gc = (unsigned)std::min<uint64_t>((c.N + CACHED_BT - 1) / CACHED_BT, (uint64_t)c.grid_c);
+      if (c.minb == 4) {
+        if (c.payload)
+          k_churn_malloc_cached<true, 4><<<gc, CACHED_BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats);
+        else
+          k_churn_malloc_cached<false, 4><<<gc, CACHED_BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats);
+      } else {
+        if (c.payload)
+          k_churn_malloc_cached<true, 2><<<gc, CACHED_BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats);
+        else
+          k_churn_malloc_cached<false, 2><<<gc, CACHED_BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats);
+      }
     } else if (c.batched & 1) {
       const int per = 1 << c.k_shift;  // requests per thread per iteration
       unsigned gk = (unsigned)std::min<uint64_t>((c.N + (uint64_t)BW * per - 1) / ((uint64_t)BW * per),
@@ -453,11 +463,13 @@ extern "C" {
  * every round but the first, then threads_per_round mallocs), then a drain of
  * all live slots; every step serves the same requests.  batched: bit 0 CTA-aggregated
  * malloc, bit 1 CTA-aggregated free (else per-thread with warp teams), bit 2
- * malloc through the CTA reservoirs (gal::res_malloc; takes precedence over
- * bit 0), bit 3 the allocator-only form (no payload written or checked),
- * bits 4-5: log2 of the requests each thread of the CTA-aggregated malloc
- * serves per iteration (0-2), bits 8-11: log2 of the reservoir run length
- * (0: 128 slices); persistent kernels; use_graph: the step is one captured
+ * malloc in persistent CTAs that cache their SM's pinned blocks
+ * (gal::malloc_cached; takes precedence over bit 0), bit 3 the allocator-only
+ * form (no payload written or checked), bits 4-5: log2 of the requests each
+ * thread of the CTA-aggregated malloc serves per iteration (0-2), bit 6: the
+ * free phase looks segment classes up in global memory instead of a copy
+ * staged in shared memory, bit 7: the cached malloc at 4 CTAs of 256 threads
+ * per SM (64 registers) instead of 2; use_graph: the step is one captured
  * CUDA graph.
  * step_ms[i]: duration of timed step i (CUDA events on the launching stream). */
 int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, uint32_t seed,
@@ -474,13 +486,9 @@ int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, 
   c.seed = seed;
   c.batched = batched & 7;
   c.payload = !(batched & 8);
+  c.minb = (batched & 128) ? 4 : 2;
   c.k_shift = (batched >> 4) & 3;
   if (c.k_shift > 2) return GAL_ERR_ARGS;
-  {
-    const int lr = (batched >> 8) & 15;
-    c.run = lr ? 1u << lr : 128u;
-    if (c.run > gal::SLICES_PER_BLOCK) return GAL_ERR_ARGS;
-  }
   c.ptrs = nullptr;
   c.live = nullptr;
   c.stats = nullptr;
@@ -496,11 +504,19 @@ int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, 
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_churn_malloc_batched<1>, BT, 0);
   c.grid_b = sms * (per_sm > 0 ? per_sm : 1);
   per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_churn_free_plain<true>, FREE_BT, 0);
+  {
+    gal_state_dims dims;
+    gal_state_dims_get(h, &dims);
+    c.stage_bytes = dims.num_segments * 2 <= gal::CLASS_STAGE_BYTES && !(batched & 64) ? dims.num_segments * 2 : 0;
+  }
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_churn_free_plain<true>, FREE_BT, c.stage_bytes);
   c.grid_f = sms * (per_sm > 0 ? per_sm : 1);
   per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_churn_malloc_res<true>, RES_BT, 0);
-  c.grid_r = sms * (per_sm > 0 ? per_sm : 1);
+  if (c.minb == 4)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_churn_malloc_cached<true, 4>, CACHED_BT, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_churn_malloc_cached<true, 2>, CACHED_BT, 0);
+  c.grid_c = sms * (per_sm > 0 ? per_sm : 1);
   c.ev.resize(2 * nkern);
   c.kind.resize(nkern);
   CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
@@ -763,7 +779,7 @@ done:
  * requests at full concurrency: malloc_cycles[i], then free_cycles[i] when the
  * same allocations are freed.  One unmeasured round first.  Host buffers.
  * batched: 0 per-thread calls, 1 CTA-aggregated claims and batched frees,
- * 2 the CTA reservoirs and batched frees. */
+ * 2 persistent CTAs with cached pinned blocks and batched frees. */
 int gal_bench_latency(gal_handle *h, uint64_t n, uint32_t seed, int batched,
                       uint32_t *malloc_cycles, uint32_t *free_cycles) {
   if (!h || !n || !malloc_cycles || !free_cycles) return GAL_ERR_ARGS;
@@ -777,15 +793,15 @@ int gal_bench_latency(gal_handle *h, uint64_t n, uint32_t seed, int batched,
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lat_malloc_batched, BT, 0);
   unsigned gb = (unsigned)std::min<uint64_t>((n + BW - 1) / BW, (uint64_t)sms * (per_sm > 0 ? per_sm : 1));
   per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lat_malloc_res, RES_BT, 0);
-  unsigned gr = (unsigned)std::min<uint64_t>((n + RES_BT - 1) / RES_BT, (uint64_t)sms * (per_sm > 0 ? per_sm : 1));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lat_malloc_cached, CACHED_BT, 0);
+  unsigned gr = (unsigned)std::min<uint64_t>((n + CACHED_BT - 1) / CACHED_BT, (uint64_t)sms * (per_sm > 0 ? per_sm : 1));
   unsigned gp = (unsigned)((n + 255) / 256);
   CK(cudaMalloc(&ptrs, n * sizeof(void *)));
   CK(cudaMalloc(&cm, n * 4));
   CK(cudaMalloc(&cf, n * 4));
   for (int r = 0; r < 2; r++) {
     if (batched == 2) {
-      k_lat_malloc_res<<<gr, RES_BT>>>(d, ptrs, 0, n, seed + r, cm);
+      k_lat_malloc_cached<<<gr, CACHED_BT>>>(d, ptrs, 0, n, seed + r, cm);
       k_lat_free_batched<<<gb, BT>>>(d, ptrs, 0, n, cf);
     } else if (batched) {
       k_lat_malloc_batched<<<gb, BT>>>(d, ptrs, 0, n, seed + r, cm);

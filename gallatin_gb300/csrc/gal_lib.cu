@@ -242,27 +242,20 @@ __global__ void k_free_per_thread(const gal::state *s, void *const *ptrs, uint64
 
 constexpr int BATCH_THREADS = 512;
 
-// BATCH_WORKERS threads claim; the CTA's last warp prepares spare blocks
-// (gal_config.spare_blocks) off the claims' path
-constexpr int BATCH_WORKERS = BATCH_THREADS - 32;
+// Batched malloc: a persistent grid of CTAs that each serve many requests per
+// thread, claiming through gal::malloc_cached: warp teams take the SM's
+// pinned block from the CTA's copy in shared memory and go to the pinned
+// slot in global memory only when the copy has gone stale.
+constexpr int MALLOC_THREADS = 256;
 
-__global__ void __launch_bounds__(BATCH_THREADS)
+__global__ void __launch_bounds__(MALLOC_THREADS)
     k_malloc_batched(const gal::state *s, const uint64_t *sizes, uint64_t n, void **out) {
-  __shared__ gal::cta_claim_smem sm;
-  gal::cta_claim_init(sm, BATCH_WORKERS);
+  __shared__ gal::slot_cache cache;
+  gal::slot_cache_init(cache);
   __syncthreads();
-  if (threadIdx.x >= BATCH_WORKERS) {
-    gal::cta_service(s, sm);
-    return;
-  }
-  for (uint64_t base = (uint64_t)blockIdx.x * BATCH_WORKERS; base < n;
-       base += (uint64_t)gridDim.x * BATCH_WORKERS) {
-    uint64_t i = base + threadIdx.x;
-    bool has = i < n;
-    void *p = gal::cta_malloc(s, has ? sizes[i] : 0, has, sm);
-    if (has) out[i] = p;
-  }
-  gal::cta_workers_done(sm);
+  for (uint64_t i = (uint64_t)blockIdx.x * MALLOC_THREADS + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * MALLOC_THREADS)
+    out[i] = gal::malloc_cached(s, sizes[i], cache);
 }
 
 // Batched free: each thread takes FREE_PER_THREAD entries per pass of a
@@ -274,7 +267,12 @@ constexpr int FREE_PER_THREAD = 4;
 
 __global__ void __launch_bounds__(BATCH_THREADS)
     k_free_batched(const gal::state *s, void *const *ptrs, uint64_t n,
-                   const unsigned long long *d_count) {
+                   const unsigned long long *d_count, int stage) {
+  // the pointers were allocated before this call, and a live pointer's
+  // segment keeps its class: a copy of the classes staged now serves them
+  extern __shared__ uint16_t classes[];
+  const bool staged = stage && gal::stage_classes(s, classes);
+  __syncthreads();
   if (d_count && *d_count < n) n = *d_count;
   // a warp takes 32 x FREE_PER_THREAD consecutive entries; lane l holds entries
   // l, l + 32, ... so neighbouring lanes hold neighbouring entries (which share
@@ -292,16 +290,16 @@ __global__ void __launch_bounds__(BATCH_THREADS)
       p[k] = i < n ? ptrs[i] : nullptr;
       go[k] = p[k] != nullptr;
     }
-    gal::free_n<FREE_PER_THREAD>(s, p, go);
+    gal::free_n<FREE_PER_THREAD>(s, p, go, staged ? classes : nullptr);
   }
 }
 
 template <class K>
-int persistent_grid(int device, K kernel) {
+int persistent_grid(int device, K kernel, int threads, size_t dyn_smem = 0) {
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, BATCH_THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, dyn_smem);
   if (per_sm < 1) per_sm = 1;
   return sms * per_sm;
 }
@@ -832,10 +830,10 @@ int gal_trim(gal_handle *h, void *stream) {
 int gal_malloc_batched(gal_handle *h, const uint64_t *sizes, uint64_t n, void **out, void *stream) {
   if (!h || (n && (!sizes || !out))) return GAL_ERR_ARGS;
   if (!n) return GAL_OK;
-  unsigned g = grid_for(n, BATCH_WORKERS);
-  if (!h->grid_malloc) h->grid_malloc = persistent_grid(h->device, k_malloc_batched);
+  unsigned g = grid_for(n, MALLOC_THREADS);
+  if (!h->grid_malloc) h->grid_malloc = persistent_grid(h->device, k_malloc_batched, MALLOC_THREADS);
   unsigned p = (unsigned)h->grid_malloc;
-  k_malloc_batched<<<g < p ? g : p, BATCH_THREADS, 0, (cudaStream_t)stream>>>(h->d_state, sizes, n, out);
+  k_malloc_batched<<<g < p ? g : p, MALLOC_THREADS, 0, (cudaStream_t)stream>>>(h->d_state, sizes, n, out);
   CUDA_TRY(cudaGetLastError());
   return GAL_OK;
 }
@@ -849,10 +847,11 @@ int gal_free_batched_n(gal_handle *h, void *const *ptrs, const unsigned long lon
   if (!h || (max_n && !ptrs)) return GAL_ERR_ARGS;
   if (!max_n) return GAL_OK;
   unsigned g = grid_for((max_n + FREE_PER_THREAD - 1) / FREE_PER_THREAD, BATCH_THREADS);
-  if (!h->grid_free) h->grid_free = persistent_grid(h->device, k_free_batched);
+  const size_t stage = h->st.num_segments * 2 <= gal::CLASS_STAGE_BYTES ? h->st.num_segments * 2 : 0;
+  if (!h->grid_free) h->grid_free = persistent_grid(h->device, k_free_batched, BATCH_THREADS, stage);
   unsigned p = (unsigned)h->grid_free;
-  k_free_batched<<<g < p ? g : p, BATCH_THREADS, 0, (cudaStream_t)stream>>>(h->d_state, ptrs, max_n,
-                                                                            d_count);
+  k_free_batched<<<g < p ? g : p, BATCH_THREADS, stage, (cudaStream_t)stream>>>(h->d_state, ptrs, max_n,
+                                                                                d_count, stage > 0);
   CUDA_TRY(cudaGetLastError());
   return GAL_OK;
 }

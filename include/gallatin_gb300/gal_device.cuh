@@ -831,10 +831,40 @@ GAL_DEVICE_INLINE char *slice_ptr(const state *s, uint32_t blk, uint64_t idx, ui
 // slices, shrinks as lanes get their slices, and every warp-wide step of an
 // attempt names it, so a team holds every caller of its class even when the
 // callers' earlier branches left them in separate groups).
+// A CTA's copy of its SM's pinned blocks, in shared memory (gal::malloc_cached):
+// per class the block last read from the class's pinned slot and that slot.
+// A copy that has gone stale (its block exhausted or replaced) shows up in the
+// claim itself -- the count comes back at or past the block's end, or with
+// another class -- and is dropped, so the next team reads the slot again.
+struct slot_cache {
+  uint32_t blk[GAL_MAX_TREES];
+  uint32_t slot[GAL_MAX_TREES];
+};
+
+// every thread of the CTA, followed by a __syncthreads()
+GAL_DEVICE_INLINE void slot_cache_init(slot_cache &c) {
+  if (threadIdx.x < GAL_MAX_TREES) {
+    c.blk[threadIdx.x] = NOBLK;
+    c.slot[threadIdx.x] = 0;
+  }
+}
+
+// A block is exhausted by exactly one claim -- the one that crosses slice
+// 4095 -- and that claim's team replaces it in its pinned slot.  A team that
+// claimed from a block it read some time before (a CTA's slot_cache, or a
+// slow team) may cross a block that has since been recycled into another
+// slot or a spare; its replace then finds its own slot holding something else
+// and does nothing, and the slot that does hold the block keeps it exhausted.
+// So a team that finds the block it has just read from its slot exhausted,
+// twice in a row, replaces it itself (a compare-and-swap on the slot, so at
+// most one replacement happens).  One thread alone never meets an exhausted
+// block in its slot, so serial offsets are unchanged.
 template <bool NAMED>
-GAL_DEVICE_INLINE void *malloc_slices(const state *s, uint32_t tree, uint32_t count, uint32_t pending) {
+GAL_DEVICE_INLINE void *malloc_slices(const state *s, uint32_t tree, uint32_t count, uint32_t pending,
+                                      slot_cache *cache = nullptr) {
   const uint32_t lane = lane_id();
   const uint64_t tid = thread_linear_id();
+  uint32_t exhausted_seen = NOBLK;  // the exhausted block this lane last read from its slot
   for (int attempt = 0; attempt < SLICE_ATTEMPTS; attempt++) {
     const uint32_t active = NAMED ? pending : active_lanes();
     const uint32_t team = __match_any_sync(active, tree) & team_group(s);
@@ -843,8 +873,19 @@ GAL_DEVICE_INLINE void *malloc_slices(const state *s, uint32_t tree, uint32_t co
     const uint32_t lt = lanemask_lt();
     // every lane of a team reads the same slot words in the same instruction
     // (one broadcast transaction), so the team needs no leader branch here
-    uint32_t seen;
-    const uint32_t slot = pick_slot(s, tree, seen);
+    uint32_t seen = NOBLK, slot = 0;
+    if (cache) {
+      seen = *(volatile uint32_t *)&cache->blk[tree];
+      slot = *(volatile uint32_t *)&cache->slot[tree];
+    }
+    const bool fresh = seen == NOBLK;  // read from the pinned slot this attempt
+    if (fresh) {
+      slot = pick_slot(s, tree, seen);
+      if (cache && seen != NOBLK) {  // every lane of the team writes the same values
+        *(volatile uint32_t *)&cache->slot[tree] = slot;
+        *(volatile uint32_t *)&cache->blk[tree] = seen;
+      }
+    }
     const uint32_t blk = __shfl_sync(active, seen, leader);
     // teams whose slot was empty retry; the rest carry on with mask `live`
     const uint32_t live = __ballot_sync(active, blk != NOBLK);
@@ -874,7 +915,16 @@ GAL_DEVICE_INLINE void *malloc_slices(const state *s, uint32_t tree, uint32_t co
       const bool should_replace = start_valid && alloc + count > SLICES_PER_BLOCK - 1;
       uint32_t leftover = start_valid ? (end_valid ? count - 1 : (uint32_t)(SLICES_PER_BLOCK - alloc)) : 0;
       if (leftover) credit_frees(s, blk, leftover);  // block_correct_frees
-      const uint32_t rep = __ballot_sync(live, should_replace) & team;
+      uint32_t rep = __ballot_sync(live, should_replace) & team;
+      const bool foreign = (uint32_t)(old >> 32) != tree;
+      const bool exhausted = !foreign && (__ballot_sync(live, start_valid) & team) == 0;
+      if (cache) {  // exhausted, replaced or foreign: the next team reads the slot again
+        if ((rep || exhausted || foreign) && (int)lane == leader) atomicCAS(&cache->blk[tree], blk, NOBLK);
+      }
+      if (exhausted && fresh) {  // the slot holds an exhausted block
+        if (exhausted_seen == blk) rep = team;  // the second time in a row: replace it here
+        exhausted_seen = blk;
+      }
       if (rep && (int)lane == leader) {
         if (s->use_spares) refill = swap_spare(s, tree, slot, blk, tid);
         else replace_block(s, tree, slot, blk, tid);
@@ -962,7 +1012,7 @@ GAL_DEVICE_COLD void *malloc_large(const state *s, uint64_t size, int block_tree
 // class and run length are selects, not branches), so single slices and runs
 // of the same class share a team.
 template <bool NAMED>
-GAL_DEVICE_INLINE void *malloc_from(const state *s, uint64_t size, uint32_t callers) {
+GAL_DEVICE_INLINE void *malloc_from(const state *s, uint64_t size, uint32_t callers, slot_cache *cache = nullptr) {
   const int T = (int)s->num_trees;
   const int bits = ceil_log2(size);
   const int t = (size >> s->min_shift) == 0 ? 0 : bits - (int)s->min_shift;
@@ -974,13 +1024,22 @@ GAL_DEVICE_INLINE void *malloc_from(const state *s, uint64_t size, uint32_t call
   const bool big = t >= T;
   const uint32_t count = 1u << (big ? t - (T - 1) : 0);
   const uint32_t tree = (uint32_t)(big ? T - 1 : t);
-  return handed_out(s, malloc_slices<NAMED>(s, tree, count, members), size);
+  return handed_out(s, malloc_slices<NAMED>(s, tree, count, members, cache), size);
 }
 
 // Gallatin::malloc as the reference calls it: each attempt's team is the lanes
 // executing it together (its coalesced_threads(), gallatin.cuh:883).
 GAL_DEVICE_INLINE void *malloc(const state *s, uint64_t size) {
   return malloc_from<false>(s, size, active_lanes());
+}
+
+// malloc for kernels whose CTAs serve many requests (persistent loops): the
+// teams take the pinned block from the CTA's slot_cache in shared memory and
+// read the pinned slot in global memory only when the copy has gone stale, so
+// a team's claim costs one L2 round trip instead of two.  Same results
+// contract as malloc.
+GAL_DEVICE_INLINE void *malloc_cached(const state *s, uint64_t size, slot_cache &cache) {
+  return malloc_from<false>(s, size, active_lanes(), &cache);
 }
 
 // malloc with the calling lanes named: every lane of `callers` calls with the
@@ -1038,8 +1097,12 @@ GAL_DEVICE_INLINE uint32_t block_of(const state *s, const void *ptr, uint16_t &t
 // Frees the pointers p[k] with go[k] set, as N calls of free() would, but
 // with their table lookups and their free-counter atomics each issued back to
 // back so the round trips overlap.  Warp teams form per k, as in free().
+// `classes`, when given, is a copy of tree_ids taken after every pointer
+// passed was allocated (see stage_classes); a live pointer's segment keeps
+// its class, so the copy answers the lookup without a trip to L2.
 template <int N>
-GAL_DEVICE_INLINE void free_n(const state *s, void *const (&p)[N], const bool (&go)[N]) {
+GAL_DEVICE_INLINE void free_n(const state *s, void *const (&p)[N], const bool (&go)[N],
+                              const uint16_t *classes = nullptr) {
   uint16_t tree[N];
   uint64_t off[N];
 #pragma unroll
@@ -1047,7 +1110,7 @@ GAL_DEVICE_INLINE void free_n(const state *s, void *const (&p)[N], const bool (&
     tree[k] = FREE_TREE;
     off[k] = go[k] ? (uint64_t)((char *)p[k] - s->memory) : 0;
     if (go[k] && (off[k] >> s->seg_shift) < s->num_segments)
-      tree[k] = ld_rlx(&s->tree_ids[off[k] >> s->seg_shift]);
+      tree[k] = classes ? classes[off[k] >> s->seg_shift] : ld_rlx(&s->tree_ids[off[k] >> s->seg_shift]);
   }
   uint32_t blk[N], old[N], cnt[N];
   bool lead[N];
@@ -1076,6 +1139,16 @@ GAL_DEVICE_INLINE void free_n(const state *s, void *const (&p)[N], const bool (&
 #pragma unroll
   for (int k = 0; k < N; k++)
     if (lead[k]) credit_done(s, blk[k], old[k], cnt[k]);
+}
+
+// Segments whose classes fit in CLASS_STAGE_BYTES of shared memory can be
+// staged for free_n: every thread of the CTA calls stage_classes, then
+// __syncthreads().  Returns false (nothing staged) for larger arenas.
+static constexpr uint32_t CLASS_STAGE_BYTES = 32768;
+GAL_DEVICE_INLINE bool stage_classes(const state *s, uint16_t *smem) {
+  if (s->num_segments * 2 > CLASS_STAGE_BYTES) return false;
+  for (uint64_t g = threadIdx.x; g < s->num_segments; g += blockDim.x) smem[g] = ld_rlx(&s->tree_ids[g]);
+  return true;
 }
 
 // a block's malloc word in the reference packing, (tree << 20) + count (block.cuh:53,220)

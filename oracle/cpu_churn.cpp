@@ -19,10 +19,11 @@
 
 extern "C" {
 
-// ops_out[0] mallocs ok, [1] mallocs failed, [2] frees; returns seconds
-double orc_churn_oracle(uint64_t arena_bytes, uint64_t threads_per_round, uint32_t rounds,
-                        uint32_t seed, uint64_t *ops_out) {
-  orc_alloc *a = orc_create(arena_bytes, 42, 16ull << 20, 16, 4096, 128, 4,
+// ops_out[0] mallocs ok, [1] mallocs failed, [2] frees; returns seconds.
+// Gallatin<segment_bytes, 16, 4096> with the reference's pinned slots.
+double orc_churn_oracle(uint64_t arena_bytes, uint64_t segment_bytes, uint64_t threads_per_round,
+                        uint32_t rounds, uint32_t seed, uint64_t *ops_out) {
+  orc_alloc *a = orc_create(arena_bytes, 42, segment_bytes, 16, 4096, 128, 4,
                             ORC_FIX_GATHER_EXIT_ROLLBACK | ORC_FIX_LEFTOVER_COMPLETES | ORC_FIX_RUN_BELOW_ARENA |
                                 ORC_FIX_RUN_RETURN_SUMMARY, 0);
   orc_boot_one_thread(a);

@@ -360,3 +360,41 @@ def test_wait_on_a_lock_nobody_releases_times_out(G, torch):
         torch.cuda.synchronize()
     finally:
         g.close()
+
+
+@pytest.mark.parametrize("mode", [4, 4 | 128, 4 | 8, 8, 4 | 64, 8 | 64])
+def test_cached_block_churn_payloads_and_fresh_trees(G, mode):
+    """Mallocs from persistent CTAs that cache their SM's pinned blocks in
+    shared memory (2 and 4 CTAs per SM), the allocator-only forms without
+    payloads, and the free phase with and without the segment classes staged
+    in shared memory: every malloc served, payloads intact, frees balance the
+    mallocs, and after trim the trees are fresh again."""
+    g = G.Gallatin.generate_on_device(32 << 30, 42, spare_blocks=1, pinned_slots_first=0,
+                                      bytes_per_segment=64 << 20, gather_unlocked_below=16)
+    try:
+        fresh = g.export()
+        N, R = 1 << 19, 6
+        ms, r = g.bench_churn(N, R, 1, mode, True, 1, 2)
+        assert r.mallocs_ok == 2 * N * R and r.mallocs_failed == 0
+        assert r.payload_mismatch == 0
+        assert r.frees == r.mallocs_ok
+        assert r.error_word == 0
+        g.trim()
+        assert g.error_word() == 0, g.error_info()
+        assert g.export().diff(fresh, fields=TREE_FIELDS) == []
+    finally:
+        g.close()
+
+
+@pytest.mark.parametrize("layout", [0, 1])
+def test_block_layouts_serve_the_same_churn(G, layout):
+    """Dense counter arrays and one 32-byte record per block: the same churn,
+    the same invariants."""
+    g = G.Gallatin.generate_on_device(16 << 30, 42, block_layout=layout)
+    try:
+        N, R = 1 << 18, 6
+        ms, r = g.bench_churn(N, R, 1, 4, True, 1, 2)
+        assert r.mallocs_ok == 2 * N * R and r.mallocs_failed == 0
+        assert r.payload_mismatch == 0 and r.frees == r.mallocs_ok and r.error_word == 0
+    finally:
+        g.close()

@@ -1,0 +1,56 @@
+"""The resident allocator server (gallatin_gb300/csrc/gal_server.cuh): three
+producer streams of different size ranges, counts and lifetimes send their
+slice requests through per-class rings to server CTAs of the same cooperative
+launch, which claim each batch's slices with one atomic per run.  Every
+request is answered, no two live allocations overlap (each carries its
+request id at both ends, checked before it is freed), each is aligned to its
+class, no wait runs out, and once everything is freed a trim leaves fresh
+trees.  The same producers calling the per-thread malloc directly keep the
+same invariants."""
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TREE_FIELDS = ["seg_tree_words", "sub_tree_words", "tree_ids", "slots", "free_counters"]
+
+# (requests, lo, hi, log-uniform, kept for this many later requests)
+STREAMS = [
+    (1_500_000, 16, 128, 0, 1),      # small objects, freed soon
+    (1_000_000, 16, 4096, 1, 2),     # the mixed 16 B - 4 KiB stream
+    (300_000, 1024, 32768, 1, 4),    # buffers, runs of 4 KiB slices among them
+]
+
+
+@pytest.fixture(scope="module")
+def G():
+    import gallatin_gb300
+    return gallatin_gb300
+
+
+@pytest.mark.parametrize("direct", [False, True], ids=["server", "direct"])
+def test_three_producer_streams(G, direct):
+    g = G.Gallatin.generate_on_device(16 << 30, 42, spare_blocks=1, pinned_slots_first=0,
+                                      bytes_per_segment=64 << 20, gather_unlocked_below=16)
+    try:
+        fresh = g.export()
+        ms, r = g.bench_server(STREAMS, server_pct=25, direct=direct, use_graph=True, warmup=1, steps=2)
+        total = sum(s[0] for s in STREAMS)
+        assert r.status == 0 and r.error_word == 0, r.as_dict()
+        assert r.mallocs_ok == 2 * total and r.mallocs_failed == 0, r.as_dict()
+        assert r.stamp_mismatch == 0 and r.misaligned == 0, r.as_dict()
+        assert r.frees == r.mallocs_ok
+        assert (r.server_ctas > 0) != direct
+        g.trim()
+        assert g.error_word() == 0, g.error_info()
+        assert g.export().diff(fresh, fields=TREE_FIELDS) == []
+    finally:
+        g.close()
+
+
+def test_server_refuses_streams_beyond_runs_of_slices(G):
+    g = G.Gallatin.generate_on_device(2 << 30, 42)
+    try:
+        with pytest.raises(G.GalError):
+            g.bench_server([(1000, 16, 1 << 20, 0, 1)])
+    finally:
+        g.close()
