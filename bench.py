@@ -93,6 +93,10 @@ def parse():
                         "class, or one thread per request")
     p.add_argument("--ctas-per-sm", type=int, default=4, choices=[2, 4],
                    help="cached form: resident CTAs of 256 threads per SM")
+    p.add_argument("--slots", type=int, default=0,
+                   help="pinned slots per class (0: one per SM); small profiling cases use fewer")
+    p.add_argument("--block-layout", default="record", choices=["record", "dense"],
+                   help="block counters: one 32-byte record per block, or dense arrays")
     p.add_argument("--quick", action="store_true", help="headline steps only (profiling)")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the secondary workloads and the reference figures beside them")
@@ -469,6 +473,8 @@ def main():
 
     N, R = args.threads_per_round, args.rounds
     arena = args.arena_gib << 30
+    TUNED["block_layout"] = 1 if args.block_layout == "record" else 0
+    TUNED["pinned_slots_first"] = TUNED["pinned_slots_min"] = args.slots
     occ_bit = 128 if args.ctas_per_sm == 4 else 0
     form_mode = {"cached": FORMS["cached"] | occ_bit, "cta": FORMS["cta"], "plain": FORMS["plain"]}
     head_mode = form_mode[args.malloc_form]

@@ -14,13 +14,32 @@
 
 namespace galwl {
 
-// stats[0] mallocs ok, [1] mallocs failed, [2] payload mismatches, [3] frees
-__device__ __forceinline__ void warp_count(unsigned long long *ctr, bool flag) {
+// Counters of a run: [0] mallocs ok, [1] mallocs failed, [2] payload
+// mismatches, [3] frees.  Every warp adds to them, so each counter is kept in
+// STAT_SHARDS copies chosen by SM, each in a 32-byte sector of its own (the
+// adds of one kernel would otherwise queue on four words); the host sums the
+// copies (stat_total).  A buffer holds STAT_WORDS 64-bit words.
+constexpr int STAT_SHARDS = 64;
+constexpr int STAT_WORDS = STAT_SHARDS * 4 * 4;
+
+__device__ __forceinline__ unsigned long long *stat_word(unsigned long long *stats, int which) {
+  uint32_t smid;
+  asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+  return stats + ((smid % STAT_SHARDS) * 4 + (uint32_t)which) * 4;
+}
+
+inline uint64_t stat_total(const unsigned long long *host_stats, int which) {
+  uint64_t t = 0;
+  for (int sh = 0; sh < STAT_SHARDS; sh++) t += host_stats[(sh * 4 + which) * 4];
+  return t;
+}
+
+__device__ __forceinline__ void warp_count(unsigned long long *stats, int which, bool flag) {
   unsigned mask;
   asm volatile("activemask.b32 %0;" : "=r"(mask));  // read once, where written
   unsigned b = __ballot_sync(mask, flag);
   int leader = __ffs(mask) - 1;
-  if ((int)(threadIdx.x & 31) == leader && b) atomicAdd(ctr, (unsigned long long)__popc(b));
+  if ((int)(threadIdx.x & 31) == leader && b) atomicAdd(stat_word(stats, which), (unsigned long long)__popc(b));
 }
 
 // Slot liveness: bit (i & 31) of live_bits[i >> 5] is set while slot i holds
@@ -50,16 +69,16 @@ __device__ __forceinline__ void churn_malloc_body(Alloc *a, void **ptrs, uint32_
   if (PAYLOAD && p) *(volatile uint32_t *)p = payload(slot, seed);
   ptrs[slot] = p;
   publish_live(live_bits, slot, p != nullptr);
-  warp_count(&stats[0], p != nullptr);
-  warp_count(&stats[1], p == nullptr);
+  warp_count(stats, 0, p != nullptr);
+  warp_count(stats, 1, p == nullptr);
 }
 
-__device__ __forceinline__ void warp_add(unsigned long long *ctr, uint32_t n) {
+__device__ __forceinline__ void warp_add(unsigned long long *stats, int which, uint32_t n) {
   unsigned mask;
   asm volatile("activemask.b32 %0;" : "=r"(mask));
   uint32_t total = __reduce_add_sync(mask, n);
   int leader = __ffs(mask) - 1;
-  if ((int)(threadIdx.x & 31) == leader && total) atomicAdd(ctr, (unsigned long long)total);
+  if ((int)(threadIdx.x & 31) == leader && total) atomicAdd(stat_word(stats, which), (unsigned long long)total);
 }
 
 // Each thread of the free phase owns FREE_SLOTS consecutive slots: one vector
@@ -205,8 +224,8 @@ __device__ __forceinline__ void churn_free_warps(Alloc *a, void **ptrs, uint32_t
     }
     __syncwarp();
   }
-  warp_add(&stats[2], nbad);
-  warp_add(&stats[3], ngo);
+  warp_add(stats, 2, nbad);
+  warp_add(stats, 3, ngo);
 }
 
 // The same selection, but the selected pointers are appended to freelist
@@ -239,8 +258,8 @@ __device__ __forceinline__ void churn_select_warps(void **ptrs, uint32_t *live_b
     }
     __syncwarp();
   }
-  warp_add(&stats[2], nbad);
-  warp_add(&stats[3], ngo);
+  warp_add(stats, 2, nbad);
+  warp_add(stats, 3, ngo);
 }
 
 }  // namespace galwl

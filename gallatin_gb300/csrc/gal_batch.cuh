@@ -80,7 +80,7 @@ static __device__ __noinline__ void cta_claim_class(const state *s, uint32_t tre
       uint32_t nx = NOBLK;
       if (s->use_spares && sm.workers != blockDim.x) nx = atomicExch(s->spares + si, NOBLK);
       if (nx != NOBLK) {  // the prepared block: one swap
-        if (atomicCAS(s->slots + si, used, nx) != used) credit_frees(s, nx, SLICES_PER_BLOCK);
+        if (atomicCAS(s->slots + si, used, nx) != used) retire_block(s, nx);
       } else {
         replace_block(s, tree, slot, used, tid);
       }
@@ -136,7 +136,7 @@ GAL_DEVICE_COLD void cta_service(const state *s, cta_claim_smem &sm) {
       const uint32_t nb = request_block(s, t, tid);
       if (nb == NOBLK) continue;
       __threadfence();
-      if (atomicCAS(s->spares + si, NOBLK, nb) != NOBLK) credit_frees(s, nb, SLICES_PER_BLOCK);
+      if (atomicCAS(s->spares + si, NOBLK, nb) != NOBLK) retire_block(s, nb);
     }
     if (*(volatile uint32_t *)&sm.stop) return;
     if (!work) __nanosleep(256);
@@ -261,9 +261,12 @@ GAL_DEVICE_COLD uint32_t claim_run(const state *s, uint32_t tree, uint32_t want,
     const uint32_t got = (uint32_t)min((uint64_t)want, (uint64_t)SLICES_PER_BLOCK - cnt);
     const bool crossed = cnt + want > SLICES_PER_BLOCK - 1;
     const bool mine = (uint32_t)(old >> 32) == tree;
-    if (!mine) credit_frees(s, blk, got);  // a foreign block: give the slices back
     const uint32_t used = blk;
-    if (crossed) {
+    if (!mine) {  // a block of another class (recycled since it was read): give the slices back
+      credit_frees(s, blk, got);
+      blk = NOBLK;
+    }
+    if (crossed && mine) {
       if (s->use_spares) {
         if (swap_spare(s, tree, slot, used, tid)) spare_slot = slot;
       } else {

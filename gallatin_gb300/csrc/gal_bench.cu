@@ -100,8 +100,8 @@ __global__ void __launch_bounds__(CACHED_BT, MINB)
     if (PAYLOAD && p) *(volatile uint32_t *)p = galwl::payload(slot, seed);
     ptrs[slot] = p;
     galwl::publish_live(live, slot, p != nullptr);
-    galwl::warp_count(&stats[0], p != nullptr);
-    galwl::warp_count(&stats[1], p == nullptr);
+    galwl::warp_count(stats, 0, p != nullptr);
+    galwl::warp_count(stats, 1, p == nullptr);
   }
 }
 
@@ -139,8 +139,8 @@ __global__ void __launch_bounds__(BT)
       if (p[k]) *(volatile uint32_t *)p[k] = galwl::payload(slot, seed);
       ptrs[slot] = p[k];
       galwl::publish_live(live, slot, p[k] != nullptr);
-      galwl::warp_count(&stats[0], p[k] != nullptr);
-      galwl::warp_count(&stats[1], p[k] == nullptr);
+      galwl::warp_count(stats, 0, p[k] != nullptr);
+      galwl::warp_count(stats, 1, p[k] == nullptr);
     }
   }
   gal::cta_workers_done(sm);
@@ -176,8 +176,8 @@ __global__ void __launch_bounds__(BT)
     }
     gal::cta_free<2 * BT * F, F>(s, p, sm);
     if (valid) galwl::clear_live(live, i0, word, sel);
-    galwl::warp_add(&stats[2], nbad);
-    galwl::warp_add(&stats[3], ngo);
+    galwl::warp_add(stats, 2, nbad);
+    galwl::warp_add(stats, 3, ngo);
   }
 }
 
@@ -189,8 +189,8 @@ __global__ void k_stamp_payload(void **ptrs, uint32_t *live, uint64_t base, uint
   void *p = ptrs[base + t];
   if (p) *(volatile uint32_t *)p = galwl::payload(base + t, seed);
   galwl::publish_live(live, base + t, p != nullptr);
-  galwl::warp_count(&stats[0], p != nullptr);
-  galwl::warp_count(&stats[1], p == nullptr);
+  galwl::warp_count(stats, 0, p != nullptr);
+  galwl::warp_count(stats, 1, p == nullptr);
 }
 
 // Appends the pointers this round frees to freelist (*count entries so far)
@@ -212,8 +212,8 @@ __global__ void k_stamp_malloc(const gal::state *s, uint64_t n, uint64_t size, u
   uint64_t *p = (uint64_t *)gal::malloc(s, size);
   if (p) p[0] = tid;
   ptrs[tid] = p;
-  galwl::warp_count(&stats[0], p != nullptr);
-  galwl::warp_count(&stats[1], p == nullptr);
+  galwl::warp_count(stats, 0, p != nullptr);
+  galwl::warp_count(stats, 1, p == nullptr);
 }
 
 __global__ void k_stamp_free(const gal::state *s, uint64_t n, uint64_t **ptrs,
@@ -226,8 +226,8 @@ __global__ void k_stamp_free(const gal::state *s, uint64_t n, uint64_t **ptrs,
     bad = p[0] != tid;
     gal::free(s, p);
   }
-  galwl::warp_count(&stats[2], bad);
-  galwl::warp_count(&stats[3], p != nullptr);
+  galwl::warp_count(stats, 2, bad);
+  galwl::warp_count(stats, 3, p != nullptr);
 }
 
 // per-request latency: clock64() around each malloc / free of one churn round
@@ -316,6 +316,16 @@ __global__ void __launch_bounds__(BT)
       ptrs[base + t] = nullptr;
       cycles[t] = (uint32_t)min(c1 - c0, 0xFFFFFFFFll);
     }
+  }
+}
+
+// the four counters of a sharded stats buffer (churn.cuh), summed; one warp
+__global__ void k_stat_reduce(const unsigned long long *stats, unsigned long long *out4) {
+  for (int which = 0; which < 4; which++) {
+    unsigned long long t = 0;
+    for (int sh = threadIdx.x; sh < galwl::STAT_SHARDS; sh += 32) t += stats[(sh * 4 + which) * 4];
+    for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xFFFFFFFFu, t, o);
+    if (threadIdx.x == 0) out4[which] = t;
   }
 }
 
@@ -527,7 +537,7 @@ int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, 
   CK(cudaMemsetAsync(c.ptrs, 0, threads_per_round * rounds * sizeof(void *), st));
   CK(cudaMalloc(&c.live, threads_per_round * rounds / 8));
   CK(cudaMemsetAsync(c.live, 0, threads_per_round * rounds / 8, st));
-  CK(cudaMalloc(&c.stats, 4 * sizeof(unsigned long long)));
+  CK(cudaMalloc(&c.stats, galwl::STAT_WORDS * sizeof(unsigned long long)));
   if (use_graph) {
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     enqueue_step(c, st, true);
@@ -535,7 +545,7 @@ int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, 
     CK(cudaGraphInstantiate(&exec, graph, 0));
   }
   for (int s = 0; s < warmup + steps; s++) {
-    CK(cudaMemsetAsync(c.stats, 0, 4 * sizeof(unsigned long long), st));
+    CK(cudaMemsetAsync(c.stats, 0, galwl::STAT_WORDS * sizeof(unsigned long long), st));
     CK(cudaStreamSynchronize(st));
     CK(cudaEventRecord(e0, st));
     if (use_graph)
@@ -561,12 +571,12 @@ int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, 
           res->free_launches++;
         }
       }
-      unsigned long long sv[4];
-      CK(cudaMemcpy(sv, c.stats, sizeof(sv), cudaMemcpyDeviceToHost));
-      res->mallocs_ok += sv[0];
-      res->mallocs_failed += sv[1];
-      res->payload_mismatch += sv[2];
-      res->frees += sv[3];
+      std::vector<unsigned long long> sv(galwl::STAT_WORDS);
+      CK(cudaMemcpy(sv.data(), c.stats, sv.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+      res->mallocs_ok += galwl::stat_total(sv.data(), 0);
+      res->mallocs_failed += galwl::stat_total(sv.data(), 1);
+      res->payload_mismatch += galwl::stat_total(sv.data(), 2);
+      res->frees += galwl::stat_total(sv.data(), 3);
     }
   }
   gal_last_error(h, &res->error_word);
@@ -609,7 +619,8 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
   void **ptrs = nullptr, **freelist[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
   uint32_t *live = nullptr;
   uint64_t *d_sizes[2] = {nullptr, nullptr};
-  unsigned long long *stats = nullptr, *count[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}}, *hst = nullptr;
+  unsigned long long *stats = nullptr, *total4 = nullptr, *hst = nullptr;
+  unsigned long long *count[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
   cudaStream_t st = nullptr, cp = nullptr, sl = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr, fork = nullptr, copied[2] = {nullptr, nullptr},
               consumed[2] = {nullptr, nullptr}, stamped = nullptr, selected[2] = {nullptr, nullptr};
@@ -626,7 +637,7 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
     return (unsigned)std::min<uint64_t>((nscan + chunk - 1) / chunk, grid_sel);
   };
   auto enqueue = [&]() -> int {
-    if (cudaMemsetAsync(stats, 0, 4 * sizeof(unsigned long long), st) != cudaSuccess) return GAL_ERR_CUDA;
+    if (cudaMemsetAsync(stats, 0, galwl::STAT_WORDS * sizeof(unsigned long long), st) != cudaSuccess) return GAL_ERR_CUDA;
     if (cudaEventRecord(fork, st) != cudaSuccess || cudaStreamWaitEvent(cp, fork, 0) != cudaSuccess ||
         cudaStreamWaitEvent(sl, fork, 0) != cudaSuccess)
       return GAL_ERR_CUDA;
@@ -677,7 +688,8 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
                                                                    seed, stats);
       if (cudaEventRecord(stamped, st) != cudaSuccess) return GAL_ERR_CUDA;
     }
-    if (cudaMemcpyAsync(hst, stats, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st) !=
+    k_stat_reduce<<<1, 32, 0, st>>>(stats, total4);  // the step's four counters, then read back
+    if (cudaMemcpyAsync(hst, total4, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st) !=
         cudaSuccess)
       return GAL_ERR_CUDA;
     return cudaGetLastError() == cudaSuccess ? GAL_OK : GAL_ERR_CUDA;
@@ -702,7 +714,8 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
   }
   CK(cudaMalloc(&ptrs, nslots * sizeof(void *)));
   CK(cudaMalloc(&live, nslots / 8));
-  CK(cudaMalloc(&stats, 4 * sizeof(unsigned long long)));
+  CK(cudaMalloc(&stats, galwl::STAT_WORDS * sizeof(unsigned long long)));
+  CK(cudaMalloc(&total4, 4 * sizeof(unsigned long long)));
   CK(cudaMallocHost(&hst, 4 * sizeof(unsigned long long)));
   CK(cudaMemsetAsync(ptrs, 0, nslots * sizeof(void *), st));
   CK(cudaMemsetAsync(live, 0, nslots / 8, st));
@@ -738,7 +751,7 @@ int gal_bench_churn_e2e(gal_handle *h, const uint64_t *host_sizes, uint64_t thre
       res->frees += hst[3];
       res->malloc_launches += rounds;
       res->free_launches += rounds;
-      res->other_launches += 3 * rounds;  // two selection parts and the stamp
+      res->other_launches += 3 * rounds + 1;  // two selection parts and the stamp a round, the count
     }
   }
   res->h2d_bytes = nslots * sizeof(uint64_t);
@@ -768,6 +781,7 @@ done:
   if (ptrs) cudaFree(ptrs);
   if (live) cudaFree(live);
   if (stats) cudaFree(stats);
+  if (total4) cudaFree(total4);
   if (hst) cudaFreeHost(hst);
   if (st) cudaStreamDestroy(st);
   if (cp) cudaStreamDestroy(cp);
@@ -842,8 +856,8 @@ int gal_bench_stamp(gal_handle *h, uint64_t n, uint64_t size, int rounds, float 
   unsigned grid = (unsigned)((n + 255) / 256);
   ms[0] = ms[1] = 0;
   CK(cudaMalloc(&ptrs, n * sizeof(void *)));
-  CK(cudaMalloc(&stats, 32));
-  CK(cudaMemset(stats, 0, 32));
+  CK(cudaMalloc(&stats, galwl::STAT_WORDS * sizeof(unsigned long long)));
+  CK(cudaMemset(stats, 0, galwl::STAT_WORDS * sizeof(unsigned long long)));
   CK(cudaEventCreate(&a));
   CK(cudaEventCreate(&b));
   CK(cudaEventCreate(&c));
@@ -861,7 +875,11 @@ int gal_bench_stamp(gal_handle *h, uint64_t n, uint64_t size, int rounds, float 
     ms[0] += x;
     ms[1] += y;
   }
-  CK(cudaMemcpy(stats_out, stats, 32, cudaMemcpyDeviceToHost));
+  {
+    std::vector<unsigned long long> sv(galwl::STAT_WORDS);
+    CK(cudaMemcpy(sv.data(), stats, sv.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < 4; i++) stats_out[i] = galwl::stat_total(sv.data(), i);
+  }
 done:
   if (a) cudaEventDestroy(a);
   if (b) cudaEventDestroy(b);

@@ -85,20 +85,14 @@ __global__ void k_boot(const gal::state *s) {
 // boot the slots again in the one-thread order.
 __global__ void k_trim(const gal::state *s) {
   if (threadIdx.x + blockIdx.x * blockDim.x != 0) return;
-  for (uint32_t i = 0; i < s->total_slots; i++) {  // spare blocks: nothing handed out
+  for (uint32_t i = 0; i < s->total_slots; i++) {  // spare blocks
     uint32_t blk = atomicExch(s->spares + i, gal::NOBLK);
-    if (blk == gal::NOBLK) continue;
-    unsigned long long old = atomicAdd(gal::mword_ptr(s, blk), (unsigned long long)gal::SLICES_PER_BLOCK);
-    uint32_t handed_out = (uint32_t)old;
-    if (handed_out < gal::SLICES_PER_BLOCK) gal::credit_frees(s, blk, gal::SLICES_PER_BLOCK - handed_out);
+    if (blk != gal::NOBLK) gal::retire_block(s, blk);
   }
   for (uint32_t t = 0; t < s->num_trees; t++)
     for (uint32_t i = 0; i < s->slot_count[t]; i++) {
       uint32_t blk = atomicExch(s->slots + s->slot_base[t] + i, gal::NOBLK);
-      if (blk == gal::NOBLK) continue;
-      unsigned long long old = atomicAdd(gal::mword_ptr(s, blk), (unsigned long long)gal::SLICES_PER_BLOCK);
-      uint32_t handed_out = (uint32_t)old;
-      if (handed_out < gal::SLICES_PER_BLOCK) gal::credit_frees(s, blk, gal::SLICES_PER_BLOCK - handed_out);
+      if (blk != gal::NOBLK) gal::retire_block(s, blk);
     }
   // segments of a class none of whose blocks is out (those gathered ahead when
   // a class took the last block of its previous segment) go back too

@@ -83,8 +83,11 @@ __global__ void __launch_bounds__(SRV_BT)
   const uint64_t slot = (uint64_t)blockIdx.x * SRV_BT + threadIdx.x;  // this lane's reply slot
   const uint64_t chunks = (st.requests + 31) / 32;
   const uint32_t keep = st.keep < KEEP_MAX ? st.keep : KEEP_MAX;
-  void *kept[KEEP_MAX];
-  uint64_t kept_id[KEEP_MAX], kept_size[KEEP_MAX];
+  // the lane's live allocations, oldest at `head`: up to `keep` of them plus
+  // the one just made
+  constexpr uint32_t RING = KEEP_MAX + 1;
+  void *kept[RING];
+  uint64_t kept_id[RING], kept_size[RING];
   uint32_t nkept = 0, head = 0;
   uint32_t ok = 0, failed = 0, bad = 0, frees = 0, misaligned = 0;
   for (uint64_t ch = (uint64_t)q * wpc + warp; ch < chunks; ch += (uint64_t)cp * wpc) {
@@ -103,9 +106,9 @@ __global__ void __launch_bounds__(SRV_BT)
       misaligned += ((uint64_t)((char *)ptr - s->memory) % (cls < largest ? cls : largest)) != 0;
       ((uint64_t *)ptr)[0] = id;
       *(uint64_t *)((char *)ptr + ((size - 8) & ~7ull)) = id;
-      kept[(head + nkept) % KEEP_MAX] = ptr;
-      kept_id[(head + nkept) % KEEP_MAX] = id;
-      kept_size[(head + nkept) % KEEP_MAX] = size;
+      kept[(head + nkept) % RING] = ptr;
+      kept_id[(head + nkept) % RING] = id;
+      kept_size[(head + nkept) % RING] = size;
       nkept++;
     } else {
       failed++;
@@ -114,7 +117,7 @@ __global__ void __launch_bounds__(SRV_BT)
       bad += !stamps_ok(kept[head], kept_size[head], kept_id[head]);
       gal::free(s, kept[head]);
       frees++;
-      head = (head + 1) % KEEP_MAX;
+      head = (head + 1) % RING;
       nkept--;
     }
   }
@@ -122,7 +125,7 @@ __global__ void __launch_bounds__(SRV_BT)
     bad += !stamps_ok(kept[head], kept_size[head], kept_id[head]);
     gal::free(s, kept[head]);
     frees++;
-    head = (head + 1) % KEEP_MAX;
+    head = (head + 1) % RING;
     nkept--;
   }
   count(&stats[0], ok);
@@ -199,7 +202,7 @@ int gal_bench_server(gal_handle *h, const gal_server_stream *streams, uint32_t n
   if (nsrv >= grid) return GAL_ERR_ARGS;
   prod = grid - nsrv;
   CK(cudaMemcpy(&hs, d, sizeof(hs), cudaMemcpyDeviceToHost));
-  r.cap_shift = 16;
+  r.cap_shift = 18;
   r.deadline_ns = (uint64_t)(deadline_ms ? deadline_ms : 5000) * 1000000ull;
   CK(cudaMalloc(&r.entries, ((uint64_t)hs.num_trees << r.cap_shift) * 8));
   CK(cudaMemset(r.entries, 0, ((uint64_t)hs.num_trees << r.cap_shift) * 8));

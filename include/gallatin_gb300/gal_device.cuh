@@ -735,6 +735,18 @@ GAL_DEVICE_INLINE void credit_done(const state *s, uint32_t blk, uint32_t old, u
   }
 }
 
+// Gives back a block this thread took for a slot or a spare and could not
+// install: closes it to further claims (its count goes past the end) and
+// credits the slices nobody claimed, so it returns to its segment now, or
+// once the slices a claim did take (one that read the block in an earlier
+// life and landed after its hand-out) are freed.  Crediting all 4,096 would
+// return it under those live slices.
+GAL_DEVICE_COLD void retire_block(const state *s, uint32_t blk) {
+  const unsigned long long old = atomicAdd(mword_ptr(s, blk), (unsigned long long)SLICES_PER_BLOCK);
+  const uint32_t handed_out = (uint32_t)old;
+  if (handed_out < SLICES_PER_BLOCK) credit_frees(s, blk, SLICES_PER_BLOCK - handed_out);
+}
+
 // Gallatin::free_offset (gallatin.cuh:1774-1827): team by block, one atomic
 GAL_DEVICE_INLINE void free_block_slices(const state *s, uint32_t blk) {
   uint32_t active = active_lanes();
@@ -774,7 +786,7 @@ GAL_DEVICE_COLD bool replace_block(const state *s, uint32_t tree, uint32_t slot,
   __threadfence();
   if (atomicCAS(sp, NOBLK, nb) != NOBLK) {
     set_error(s, GAL_DEV_ERR_SLOT_SWAP);
-    credit_frees(s, nb, SLICES_PER_BLOCK);  // hand the unused block back
+    retire_block(s, nb);  // hand the block back
     return false;
   }
   return true;
@@ -791,7 +803,7 @@ GAL_DEVICE_COLD bool swap_spare(const state *s, uint32_t tree, uint32_t slot, ui
   if (nx == NOBLK) {
     replace_block(s, tree, slot, blk, tid);
   } else if (atomicCAS(s->slots + si, blk, nx) != blk) {
-    credit_frees(s, nx, SLICES_PER_BLOCK);  // the slot moved on: give the spare back
+    retire_block(s, nx);  // the slot moved on: give the spare back
     return false;
   }
   return true;
@@ -802,7 +814,7 @@ GAL_DEVICE_COLD void refill_spare(const state *s, uint32_t tree, uint32_t slot, 
   const uint32_t nb = request_block(s, tree, tid);
   if (nb == NOBLK) return;
   __threadfence();
-  if (atomicCAS(s->spares + si, NOBLK, nb) != NOBLK) credit_frees(s, nb, SLICES_PER_BLOCK);
+  if (atomicCAS(s->spares + si, NOBLK, nb) != NOBLK) retire_block(s, nb);
 }
 
 // Gallatin::boot_block (gallatin.cuh:726-787)
@@ -855,16 +867,19 @@ GAL_DEVICE_INLINE void slot_cache_init(slot_cache &c) {
 // slow team) may cross a block that has since been recycled into another
 // slot or a spare; its replace then finds its own slot holding something else
 // and does nothing, and the slot that does hold the block keeps it exhausted.
-// So a team that finds the block it has just read from its slot exhausted,
-// twice in a row, replaces it itself (a compare-and-swap on the slot, so at
-// most one replacement happens).  One thread alone never meets an exhausted
-// block in its slot, so serial offsets are unchanged.
+// Every failed claim still adds to the block's count, so a block left
+// exhausted in a slot soon reads far past its end: a team that reads its
+// slot's block more than STUCK_MARGIN slices past the end replaces it itself
+// (a compare-and-swap on the slot, so at most one replacement happens).  The
+// rightful crosser swaps its block within a few claims of the end, so the
+// margin keeps the teams out of each other's way.  One thread alone never
+// meets an exhausted block in its slot, so serial offsets are unchanged.
+static constexpr uint32_t STUCK_MARGIN = 1u << 12;
 template <bool NAMED>
 GAL_DEVICE_INLINE void *malloc_slices(const state *s, uint32_t tree, uint32_t count, uint32_t pending,
                                       slot_cache *cache = nullptr) {
   const uint32_t lane = lane_id();
   const uint64_t tid = thread_linear_id();
-  uint32_t exhausted_seen = NOBLK;  // the exhausted block this lane last read from its slot
   for (int attempt = 0; attempt < SLICE_ATTEMPTS; attempt++) {
     const uint32_t active = NAMED ? pending : active_lanes();
     const uint32_t team = __match_any_sync(active, tree) & team_group(s);
@@ -921,10 +936,8 @@ GAL_DEVICE_INLINE void *malloc_slices(const state *s, uint32_t tree, uint32_t co
       if (cache) {  // exhausted, replaced or foreign: the next team reads the slot again
         if ((rep || exhausted || foreign) && (int)lane == leader) atomicCAS(&cache->blk[tree], blk, NOBLK);
       }
-      if (exhausted && fresh) {  // the slot holds an exhausted block
-        if (exhausted_seen == blk) rep = team;  // the second time in a row: replace it here
-        exhausted_seen = blk;
-      }
+      if (exhausted && fresh && (old & 0xFFFFFFFFull) >= SLICES_PER_BLOCK + STUCK_MARGIN)
+        rep = team;  // the slot has held an exhausted block for a while: replace it here
       if (rep && (int)lane == leader) {
         if (s->use_spares) refill = swap_spare(s, tree, slot, blk, tid);
         else replace_block(s, tree, slot, blk, tid);

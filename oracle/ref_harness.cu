@@ -336,8 +336,8 @@ extern "C" __global__ void ref_stamp_malloc(ref_type *a, uint64_t n, uint64_t si
   uint64_t *p = (uint64_t *)a->malloc(size);
   if (p) p[0] = tid;
   ptrs[tid] = p;
-  galwl::warp_count(&stats[0], p != nullptr);
-  galwl::warp_count(&stats[1], p == nullptr);
+  galwl::warp_count(stats, 0, p != nullptr);
+  galwl::warp_count(stats, 1, p == nullptr);
 }
 
 extern "C" __global__ void ref_stamp_free(ref_type *a, uint64_t n, uint64_t **ptrs,
@@ -351,8 +351,8 @@ extern "C" __global__ void ref_stamp_free(ref_type *a, uint64_t n, uint64_t **pt
     a->free(p);
     ptrs[tid] = nullptr;
   }
-  galwl::warp_count(&stats[2], bad);
-  galwl::warp_count(&stats[3], p != nullptr);
+  galwl::warp_count(stats, 2, bad);
+  galwl::warp_count(stats, 3, p != nullptr);
 }
 
 // one thread per request through the reference's per-thread malloc / free

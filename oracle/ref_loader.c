@@ -29,6 +29,18 @@
 static CUcontext g_ctx;
 static int g_init = 0;
 
+/* the churn's counters, four of them each in STAT_SHARDS copies one sector
+ * apart (the layout of galwl::stat_word in gallatin_gb300/csrc/churn.cuh) */
+#define STAT_SHARDS 64
+#define STAT_BYTES (STAT_SHARDS * 4 * 4 * 8)
+static void stat_totals(const unsigned long long *buf, unsigned long long *out4) {
+  for (int which = 0; which < 4; which++) {
+    unsigned long long t = 0;
+    for (int sh = 0; sh < STAT_SHARDS; sh++) t += buf[(sh * 4 + which) * 4];
+    out4[which] = t;
+  }
+}
+
 /* one loaded cubin: the reference built for one Gallatin<seg, min, max> */
 typedef struct {
   char path[1024];
@@ -285,14 +297,15 @@ int ref_churn(void *h, uint64_t threads_per_round, uint32_t rounds, uint32_t see
   CK(cuMemsetD8(ptrs, 0, nslots * 8));
   CK(cuMemAlloc(&live, nslots / 8));
   CK(cuMemsetD8(live, 0, nslots / 8));
-  CK(cuMemAlloc(&stats, 32));
+  CK(cuMemAlloc(&stats, STAT_BYTES));
   CUevent e0, e1;
   CK(cuEventCreate(&e0, CU_EVENT_DEFAULT));
   CK(cuEventCreate(&e1, CU_EVENT_DEFAULT));
   unsigned block = 256;
   memset(stats_out, 0, 4 * sizeof(unsigned long long));
+  unsigned long long *hbuf = (unsigned long long *)malloc(STAT_BYTES);
   for (int s = 0; s < warmup + steps; s++) {
-    CK(cuMemsetD8(stats, 0, 32));
+    CK(cuMemsetD8(stats, 0, STAT_BYTES));
     CK(cuCtxSynchronize());
     CK(cuEventRecord(e0, 0));
     for (uint32_t rd = 0; rd < rounds; rd++) {
@@ -322,10 +335,12 @@ int ref_churn(void *h, uint64_t threads_per_round, uint32_t rounds, uint32_t see
     if (s >= warmup) {
       out_ms[s - warmup] = ms;
       unsigned long long st[4];
-      CK(cuMemcpyDtoH(st, stats, 32));
+      CK(cuMemcpyDtoH(hbuf, stats, STAT_BYTES));
+      stat_totals(hbuf, st);
       for (int i = 0; i < 4; i++) stats_out[i] += st[i];
     }
   }
+  free(hbuf);
   CK(cuEventDestroy(e0));
   CK(cuEventDestroy(e1));
   CK(cuMemFree(ptrs));
@@ -342,8 +357,8 @@ int ref_stamp(void *h, uint64_t n, uint64_t size, int rounds, float *out_ms,
   CUdeviceptr ptrs, stats;
   CK(cuMemAlloc(&ptrs, n * 8));
   CK(cuMemsetD8(ptrs, 0, n * 8));
-  CK(cuMemAlloc(&stats, 32));
-  CK(cuMemsetD8(stats, 0, 32));
+  CK(cuMemAlloc(&stats, STAT_BYTES));
+  CK(cuMemsetD8(stats, 0, STAT_BYTES));
   CUevent e0, e1, e2;
   CK(cuEventCreate(&e0, CU_EVENT_DEFAULT));
   CK(cuEventCreate(&e1, CU_EVENT_DEFAULT));
@@ -368,7 +383,12 @@ int ref_stamp(void *h, uint64_t n, uint64_t size, int rounds, float *out_ms,
     out_ms[0] += a;
     out_ms[1] += b;
   }
-  CK(cuMemcpyDtoH(stats_out, stats, 32));
+  {
+    unsigned long long *hbuf = (unsigned long long *)malloc(STAT_BYTES);
+    CK(cuMemcpyDtoH(hbuf, stats, STAT_BYTES));
+    stat_totals(hbuf, stats_out);
+    free(hbuf);
+  }
   CK(cuMemFree(ptrs));
   CK(cuMemFree(stats));
   return 0;

@@ -111,4 +111,15 @@ def test_null_arguments_rejected(L):
     assert L.gal_get_stats(None, None) == G._abi.GAL_ERR_ARGS
     assert L.gal_replay_trace(None, None, 0, None, None, None) == G._abi.GAL_ERR_ARGS
     assert L.gal_replay_warp_trace(None, None, 0, None, None, None) == G._abi.GAL_ERR_ARGS
+    assert L.gal_export_state_noalloc(None, None) == G._abi.GAL_ERR_ARGS
+    assert L.gal_job_launch(None, 0, 0, 0, None, None, None) == G._abi.GAL_ERR_ARGS
+    assert L.gal_bench_server(None, None, 0, 0, 0, 0, 0, 0, 0, None, None) == G._abi.GAL_ERR_ARGS
     assert L.gal_global() is None
+
+
+def test_job_grid_rule_matches_the_host_mirror(L):
+    """gal_job_ctas and the served loop's admission estimate agree."""
+    from gallatin_gb300.serve import job_ctas
+    for kind in (0, 1):
+        for n in (1, 1000, 1 << 18, 3 << 18, 1 << 20, 5 << 20, 1 << 24, 1 << 30):
+            assert L.gal_job_ctas(kind, n) == job_ctas(kind, n)

@@ -398,3 +398,28 @@ def test_block_layouts_serve_the_same_churn(G, layout):
         assert r.payload_mismatch == 0 and r.frees == r.mallocs_ok and r.error_word == 0
     finally:
         g.close()
+
+
+@pytest.mark.parametrize("spares", [0, 1])
+def test_exhausted_block_left_in_a_slot_is_replaced(G, torch, spares):
+    """A pinned slot that holds a block whose slices are all handed out, with
+    no claim left to cross its end (what a stale claim on a recycled block can
+    leave behind), is replaced by the next team that finds it there twice:
+    the request is served from a new block and nothing is reported."""
+    g = G.Gallatin.generate_on_device(2 << 30, 42, spare_blocks=spares, smid_override=0)
+    try:
+        sv = g.export()
+        blk = int(sv.slots_of(0)[0])            # the block pinned in class 0, slot 0
+        # exhausted long ago: every slice handed out and many claims failed since
+        sv.malloc_counters[blk] = (0 << 20) | (4096 + (1 << 12))
+        g.load(sv)
+        sizes = torch.full((1,), 16, dtype=torch.int64, device="cuda")
+        ptrs = torch.zeros(1, dtype=torch.int64, device="cuda")
+        g.malloc_per_thread(sizes, ptrs)
+        torch.cuda.synchronize()
+        assert int(ptrs.item()) != 0
+        after = g.export()
+        assert int(after.slots_of(0)[0]) != blk
+        assert g.error_word() == 0, g.error_info()
+    finally:
+        g.close()

@@ -29,7 +29,7 @@ def G():
 
 @pytest.mark.parametrize("direct", [False, True], ids=["server", "direct"])
 def test_three_producer_streams(G, direct):
-    g = G.Gallatin.generate_on_device(16 << 30, 42, spare_blocks=1, pinned_slots_first=0,
+    g = G.Gallatin.generate_on_device(64 << 30, 42, spare_blocks=1, pinned_slots_first=0,
                                       bytes_per_segment=64 << 20, gather_unlocked_below=16)
     try:
         fresh = g.export()
