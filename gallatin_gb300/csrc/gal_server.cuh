@@ -94,16 +94,6 @@ GAL_DEVICE_INLINE void *server_malloc(const state *s, const server_rings &r, uin
   return v == 1ull ? nullptr : (void *)v;
 }
 
-struct server_smem {
-  run_cache runs;                    // the block of each class's last run
-  unsigned long long first;          // first position of the batch
-  uint32_t count;                    // requests in the batch
-  uint32_t nruns;
-  uint32_t run_blk[SERVER_RUNS], run_start[SERVER_RUNS], run_len[SERVER_RUNS];
-  uint32_t spare_slot[SERVER_RUNS];
-  uint32_t served, stop;
-};
-
 // Takes up to `most` positions of class t that producers have reserved;
 // returns how many (first position in *first).  One thread.
 GAL_DEVICE_INLINE uint32_t server_take(const server_rings &r, uint32_t t, uint32_t most, unsigned long long *first) {
@@ -123,41 +113,58 @@ GAL_DEVICE_INLINE uint32_t server_take(const server_rings &r, uint32_t t, uint32
   return 0;
 }
 
-// The server loop of one CTA (every thread calls it): sweeps the classes,
-// serves a batch of up to blockDim.x requests of a class at a time, and
-// returns once no producer is left and every reserved position is served,
-// or at the deadline.
+// Per server warp, the block of each class's last run (shared memory).
+struct server_smem {
+  run_cache runs[32];  // indexed by warp within the CTA (up to 1,024 threads)
+};
+
+// The server loop (every thread of a server CTA calls it).  Each warp serves
+// on its own, without CTA barriers: it sweeps the classes, starting at a
+// class of its own, takes a batch of up to 32 reserved positions of a class,
+// claims their slices with one atomicAdd per run (lane 0), and every lane
+// answers one request.  Returns once no producer is left and every reserved
+// position is served, or at the deadline.
 GAL_DEVICE_INLINE void server_loop(const state *s, const server_rings &r, server_smem &sm, uint64_t t0) {
   const uint32_t T = s->num_trees;
-  run_cache_init(sm.runs);
-  if (threadIdx.x == 0) sm.stop = 0;
-  if (threadIdx.x < SERVER_RUNS) sm.spare_slot[threadIdx.x] = NOBLK;
-  __syncthreads();
+  const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+  run_cache &rc = sm.runs[warp];
+  if (lane < GAL_MAX_TREES) {
+    rc.blk[lane] = NOBLK;
+    rc.slot[lane] = 0;
+  }
+  __syncwarp();
+  const uint32_t first_class = (blockIdx.x * (blockDim.x >> 5) + warp) % T;
   for (uint32_t sweep = 0;; sweep++) {
-    if (threadIdx.x == 0) sm.served = 0;
+    uint32_t served = 0;
     for (uint32_t k = 0; k < T; k++) {
-      const uint32_t t = (k + blockIdx.x) % T;  // servers start their sweeps on different classes
-      if (threadIdx.x == 0) {
-        sm.count = server_take(r, t, blockDim.x, &sm.first);
-        sm.nruns = 0;
-        uint32_t need = sm.count;
-        while (need && sm.nruns < SERVER_RUNS) {  // one atomicAdd per run on the pinned block
-          uint32_t blk, start, spare_slot;
-          const uint32_t got = claim_run(s, t, need, sm.runs, blk, start, spare_slot);
-          sm.spare_slot[sm.nruns] = spare_slot;
+      const uint32_t t = (first_class + k) % T;
+      unsigned long long first = 0;
+      uint32_t m = 0, nruns = 0, spare_slot[2] = {NOBLK, NOBLK};
+      uint32_t rb[2] = {NOBLK, NOBLK}, rs[2] = {0, 0}, rl[2] = {0, 0};
+      if (lane == 0) {
+        m = server_take(r, t, 32, &first);
+        uint32_t need = m;
+        while (need && nruns < 2) {  // 32 slices: at most one crossing of a block's end
+          uint32_t blk, start, ss;
+          const uint32_t got = claim_run(s, t, need, rc, blk, start, ss);
+          spare_slot[nruns] = ss;
           if (!got) break;
-          sm.run_blk[sm.nruns] = blk;
-          sm.run_start[sm.nruns] = start;
-          sm.run_len[sm.nruns] = got;
-          sm.nruns++;
+          rb[nruns] = blk;
+          rs[nruns] = start;
+          rl[nruns] = got;
+          nruns++;
           need -= got;
         }
-        sm.served += sm.count;
       }
-      __syncthreads();
-      const uint32_t m = sm.count;
-      if (threadIdx.x < m) {
-        const uint64_t pos = sm.first + threadIdx.x;
+      m = __shfl_sync(0xFFFFFFFFu, m, 0);
+      if (m == 0) continue;
+      served += m;
+      first = __shfl_sync(0xFFFFFFFFu, first, 0);
+      const uint32_t b0 = __shfl_sync(0xFFFFFFFFu, rb[0], 0), b1 = __shfl_sync(0xFFFFFFFFu, rb[1], 0);
+      const uint32_t s0 = __shfl_sync(0xFFFFFFFFu, rs[0], 0), s1 = __shfl_sync(0xFFFFFFFFu, rs[1], 0);
+      const uint32_t l0 = __shfl_sync(0xFFFFFFFFu, rl[0], 0), l1 = __shfl_sync(0xFFFFFFFFu, rl[1], 0);
+      if (lane < m) {
+        const uint64_t pos = first + lane;
         unsigned long long *e = r.entries + ((uint64_t)t << r.cap_shift) + (pos & ((1ull << r.cap_shift) - 1));
         const unsigned long long lap = (pos >> r.cap_shift) & 0xFFFFFFull;
         unsigned long long v;
@@ -171,39 +178,30 @@ GAL_DEVICE_INLINE void server_loop(const state *s, const server_rings &r, server
           __nanosleep(i < 4 ? 32 : 256);
         }
         if (ok) {
-          uint32_t j = threadIdx.x;
           void *p = nullptr;
-          for (uint32_t q = 0; q < sm.nruns; q++) {
-            if (j < sm.run_len[q]) {
-              p = slice_ptr(s, sm.run_blk[q], sm.run_start[q] + j, t);
-              break;
-            }
-            j -= sm.run_len[q];
-          }
-          if (!p) p = malloc_slices<false>(s, t, 1, active_lanes());  // the runs fell short
+          if (lane < l0) p = slice_ptr(s, b0, s0 + lane, t);
+          else if (lane < l0 + l1) p = slice_ptr(s, b1, s1 + lane - l0, t);
+          else p = malloc_slices<false>(s, t, 1, active_lanes());  // the runs fell short
           if (p && s->zero_fill) zero_fill(p, 1ull << (s->min_shift + t));  // the whole slice
           const uint64_t slot = (v & ((1ull << 40) - 1)) - 1;
           st_release(e, 0ull);  // the entry is free for the next lap
           st_release(r.reply + slot, p ? (unsigned long long)p : 1ull);
         }
       }
-      __syncthreads();
-      if (threadIdx.x == 0)  // spare blocks of the runs that crossed a block's end
-        for (uint32_t q = 0; q <= sm.nruns && q < SERVER_RUNS; q++)
-          if (sm.spare_slot[q] != NOBLK) {
-            refill_spare(s, t, sm.spare_slot[q], thread_linear_id());
-            sm.spare_slot[q] = NOBLK;
-          }
+      __syncwarp();
+      if (lane == 0)  // spare blocks of the runs that crossed a block's end, after the replies
+        for (int q = 0; q < 2; q++)
+          if (spare_slot[q] != NOBLK) refill_spare(s, t, spare_slot[q], thread_linear_id());
     }
-    if (threadIdx.x == 0) {
+    int stop = 0;
+    if (lane == 0) {
       bool done = ld_rlx(r.producers_left) == 0u;
       for (uint32_t t = 0; done && t < T; t++)
         done = ld_acquire(r.taken + (uint64_t)t * 4) >= ld_acquire(r.tail + (uint64_t)t * 4);
-      if (done || global_ns() - t0 > r.deadline_ns) sm.stop = 1;
-      else if (sm.served == 0) __nanosleep(256);
+      stop = done || global_ns() - t0 > r.deadline_ns;
+      if (!stop && served == 0) __nanosleep(256);
     }
-    __syncthreads();
-    if (sm.stop) break;
+    if (__shfl_sync(0xFFFFFFFFu, stop, 0)) break;
   }
 }
 
