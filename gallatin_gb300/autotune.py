@@ -9,7 +9,9 @@ ranks them by malloc+free ops/s:
   max_size           {4096, 16384} B
   pinned slots       {one per SM, 128 halving to 4}   (block-buffer breadth)
   gather_unlocked_below {0, 16}            (classes that gather without a lock)
-  free aggregation   {warp team, CTA}      (aggregation width of frees)
+  malloc form        {per-thread teams, one CTA claim per class, persistent
+                      CTAs with the pinned blocks cached in shared memory}
+                                           (aggregation width of the claims)
   spare blocks       {off, on}             (block-buffer depth: a prepared next
                                             block per pinned slot)
 
@@ -28,12 +30,16 @@ ARENA = 128 << 30
 
 
 def grid():
-    for seg, mn, mx, slots, unlocked, free_mode, spares in itertools.product(
-            (16, 64), (16, 128), (4096, 16384), (0, 128), (0, 16), ("warp", "cta"), (0, 1)):
+    for seg, mn, mx, slots, unlocked, form, spares in itertools.product(
+            (16, 64), (16, 128), (4096, 16384), (0, 128), (0, 16), ("plain", "cta", "cached"), (0, 1)):
         if (seg << 20) < mx * 4096:
             continue
         yield dict(segment_mib=seg, min_size=mn, max_size=mx, slots=slots, unlocked=unlocked,
-                   free_mode=free_mode, spares=spares)
+                   form=form, spares=spares)
+
+
+# gal_bench_churn modes of the malloc forms (frees: warp teams, classes staged)
+FORM_MODES = {"plain": 0, "cta": 1, "cached": 4}
 
 
 def run_one(G, knobs, n, rounds, steps, seed=1):
@@ -45,7 +51,7 @@ def run_one(G, knobs, n, rounds, steps, seed=1):
         cfg["pinned_slots_min"] = 4
     g = G.Gallatin.generate_on_device(ARENA, 42, **cfg)
     try:
-        mode = 1 | (2 if knobs["free_mode"] == "cta" else 0)
+        mode = FORM_MODES[knobs["form"]]
         _, r = g.bench_churn(n, rounds, seed, batched=mode, use_graph=True, warmup=1, steps=steps)
         ok = r.mallocs_failed == 0 and r.payload_mismatch == 0 and r.error_word == 0
         return {"knobs": knobs, "ops_per_s": (r.mallocs_ok + r.frees) / (r.ms_total / 1e3),

@@ -13,7 +13,7 @@ def test_grid_is_legal_and_complete():
     geoms = {(k["segment_mib"], k["min_size"], k["max_size"]) for k in g}
     assert geoms == {(16, 16, 4096), (16, 128, 4096), (64, 16, 4096), (64, 128, 4096),
                      (64, 16, 16384), (64, 128, 16384)}
-    assert {k["free_mode"] for k in g} == {"warp", "cta"}
+    assert {k["form"] for k in g} == set(autotune.FORM_MODES)
     assert len(g) == len({tuple(sorted(k.items())) for k in g})
 
 
