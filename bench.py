@@ -305,6 +305,16 @@ def run_reference(args, world, rank):
     return line
 
 
+# The reference build is not run on the large/block workload: when a run of
+# segments cannot be found, its search ends by setting bits of the segment
+# tree's first word that no try had cleared (veb.cuh:447), marking segments in
+# use as free; the next claim of such a segment hits one of its trap
+# instructions (gallatin.cuh:1488), and a trap ends the GPU context.  This
+# workload refuses run requests at its fill margin, so it would reach that.
+REFERENCE_LARGE_UNAVAILABLE = ("unavailable: the reference's failed segment-run search marks in-use "
+                               "segments free (veb.cuh:447) and its next claim traps (gallatin.cuh:1488)")
+
+
 def reference_configs(only):
     """The reference build on the secondary workloads it has a path for: the
     1 Mi x 16 B tid stamp (its global_test flow) and the large and block-size
@@ -323,12 +333,7 @@ def reference_configs(only):
                         "malloc_ms": float(rms[0]) / 20, "free_ms": float(rms[1]) / 20,
                         "stamp_errors": int(rst[2]), "failed": int(rst[1]), "rounds": 20}
     if "large" in only:
-        from gallatin_gb300.workloads import large_block_workload
-        ref = refgpu.RefGPU(64 << 30, 7, refgpu.BOOT_RACY)
-        try:
-            out["large"] = large_block_workload(refgpu.LargeBlockBackend(ref, 7))
-        finally:
-            ref.close()
+        out["large"] = REFERENCE_LARGE_UNAVAILABLE
     return out
 
 
@@ -640,9 +645,9 @@ def main():
         configs["3_large"] = {"ours": ours_large(G)}
         served = ours_served(G)
         configs["5_served"] = {"ours": {k: served[k] for k in served if k != "checksums"}}
-        ref = reference_configs_subprocess(["stamp", "large"])
+        ref = reference_configs_subprocess(["stamp"])
         configs["1_stamp"]["reference"] = ref.get("stamp", ref.get("unavailable"))
-        configs["3_large"]["reference"] = ref.get("large", ref.get("unavailable"))
+        configs["3_large"]["reference"] = REFERENCE_LARGE_UNAVAILABLE
         configs["5_served"]["reference"] = ("n/a: the reference's queue (data_structs/queue.cuh) does not "
                                             "compile with nvcc 13")
 
