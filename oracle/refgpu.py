@@ -163,37 +163,3 @@ class RefGPU:
             raise RuntimeError(f"ref_stamp failed ({r})")
         return ms, st
 
-
-class LargeBlockBackend:
-    """The reference build as a backend of
-    gallatin_gb300.workloads.large_block_workload: per-thread malloc/free of
-    request batches, and the free runs of its segment tree for the
-    fragmentation figure."""
-
-    def __init__(self, ref: RefGPU, seed):
-        from oracle.oracle import Oracle
-        self.ref = ref
-        self.arena_bytes = ref.num_bytes // ref.segment_bytes * ref.segment_bytes
-        self.arena_base = ref.arena_base
-        self.dims = Oracle(ref.num_bytes, seed, boot=False).dims()
-
-    def malloc(self, sizes):
-        return self.ref.malloc_sizes(sizes)
-
-    def free(self, ptrs):
-        return self.ref.free_ptrs(np.asarray(ptrs).view(np.uint64))
-
-    def free_runs(self):
-        from gallatin_gb300.workloads import largest_run_of_ones
-        sv = self.ref.export(self.dims)
-        S = int(self.dims.num_segments)
-        bottom = sv.seg_tree_words[-((S + 63) // 64):]
-        free = int(sum(bin(int(w)).count("1") for w in bottom))
-        return largest_run_of_ones(bottom, S), free
-
-    def extra(self):
-        sv = self.ref.export(self.dims)
-        T = int(self.dims.num_trees)
-        ids = sv.tree_ids.astype(np.int64)
-        return {"multi_segment_allocs_after_drain": int(((ids > T) & (ids != 0xFFFF)).sum()),
-                "error_word": None}
