@@ -112,3 +112,27 @@ def test_trim_on_a_full_arena_tries_every_slot():
         o.free(x)
     o.trim()
     assert o.export().diff(fresh, fields=TREE_FIELDS) == []
+
+
+def test_failed_run_search_marks_in_use_segments_free_in_reference():
+    """veb.cuh:447: when no run is found, the reference's search sets the low
+    bits of the segment tree's first word that its last try had taken from
+    another word, although that try already gave them back.  On 128 segments:
+    segment 0 holds a whole block, a run of 63 takes 65-127, and a run of 65
+    fails after trying segment 64 with the top of word 0 -- the reference then
+    lists segment 0 as free while it is in use (its next claim would trap,
+    gallatin.cuh:1488); the product leaves the tree as it was."""
+    from gallatin_gb300._abi import FAIL
+    from oracle.oracle import FIX_GATHER_EXIT_ROLLBACK, PRODUCT_FIXES, Oracle
+    seg = 16 << 20
+    free_bit0 = {}
+    for name, fixes in (("reference", PRODUCT_FIXES & ~FIX_GATHER_EXIT_ROLLBACK), ("product", PRODUCT_FIXES)):
+        o = Oracle(2 << 30, 42, fixes=fixes, boot=False)
+        assert o.malloc(seg) == 0                  # segment 0, class of 16 MiB blocks
+        o.free(o.malloc(64 * seg))
+        assert o.malloc(63 * seg) == 65 * seg
+        assert o.malloc(65 * seg) == FAIL
+        sv = o.export()
+        assert sv.tree_ids[0] != 0xFFFF             # segment 0 is in use
+        free_bit0[name] = bool(int(sv.seg_tree_words[1]) & 1)   # bottom word 0, bit 0
+    assert free_bit0 == {"reference": True, "product": False}
