@@ -449,6 +449,14 @@ def run_configs(impl, only):
 
 
 # ---------------------------------------------------------------- our arm
+_T0 = time.time()
+
+
+def progress(what):
+    """One line on stderr per phase, with the seconds since start."""
+    print(f"[bench {time.time() - _T0:7.1f} s] {what}", file=sys.stderr, flush=True)
+
+
 def churn_value(res):
     return (res.mallocs_ok + res.frees) / (res.ms_total / 1e3)
 
@@ -512,6 +520,7 @@ def main():
                               "result": res.as_dict()}))
         return
 
+    progress("headline done")
     # end to end through the public C ABI with host-resident request sizes
     sizes = torch.empty(N * R, dtype=torch.int64, pin_memory=True)
     sizes.numpy()[:] = G.churn_sizes(0, N * R, SEED).view(np.int64)
@@ -535,6 +544,7 @@ def main():
     # per free, plus 4 B of liveness word per 32 slots scanned.  L2 atomics:
     # one counter atomic per request (the per-block malloc or free counter)
     # against the atomic peak measured in this run.
+    progress("e2e done")
     distinct, same = G.atomic_peak()
     hbm_peak, peak_src = measured_hbm_peak()
     malloc_kern = {"cached": "k_churn_malloc_cached", "cta": "k_churn_malloc_batched",
@@ -581,7 +591,10 @@ def main():
                 "malloc_p99_cycles": float(np.percentile(mc, 99)),
                 "free_p50_cycles": float(np.percentile(fc, 50)),
                 "free_p99_cycles": float(np.percentile(fc, 99))}
-    latency = {"requests": N, "cached": lat(g, 2), "cta_claim": lat(g, 1), "plain_tuned_knobs": lat(g, 0)}
+    latency = {"requests": N}
+    for key, b in (("cached", 2), ("cta_claim", 1), ("plain_tuned_knobs", 0)):
+        latency[key] = lat(g, b)
+        progress(f"latency {key} done")
     g.close()
 
     # every malloc form at the same knobs, full churn and allocator-only churn
@@ -596,6 +609,7 @@ def main():
                 errors |= rf.error_word | (0 if churn_ok(rf) else 1 << 31)
             finally:
                 gf.close()
+            progress(f"form {name} {key} done")
             v = churn_value(rf)
             step_ms = rf.ms_total / steps_f
             mall = rf.mallocs_ok / steps_f
@@ -615,6 +629,7 @@ def main():
 
     # the per-thread path at the reference's default knobs (128 pinned slots
     # halving to 4, 16 MiB segments, no spare blocks)
+    progress("forms done")
     gp = G.Gallatin.generate_on_device(arena, ALLOC_SEED)
     _, plain = gp.bench_churn(N, R, SEED, batched=False, use_graph=False, warmup=1, steps=max(1, args.steps // 3))
     plain_v = churn_value(plain)
@@ -623,6 +638,7 @@ def main():
     gp.close()
 
     # the resident server against the same producers calling malloc directly
+    progress("plain default knobs done")
     server = {}
     if world == 1:
         for key, direct in (("server", False), ("direct", True)):
@@ -636,16 +652,21 @@ def main():
                            "ms_per_step": sr.ms_total / 3, "violations": int(sr.stamp_mismatch + sr.misaligned),
                            "failed": int(sr.mallocs_failed), "status": int(sr.status),
                            "grid": int(sr.grid), "server_ctas": int(sr.server_ctas), "graph": bool(sr.graph)}
+            progress(f"server {key} done")
         server["streams"] = [list(s) for s in SERVER_STREAMS]
 
     # secondary workloads, ours and the reference build's
     configs = {}
     if world == 1 and not args.no_extras:
         configs["1_stamp"] = {"ours": ours_stamp(G)}
+        progress("stamp done")
         configs["3_large"] = {"ours": ours_large(G)}
+        progress("large done")
         served = ours_served(G)
+        progress("served done")
         configs["5_served"] = {"ours": {k: served[k] for k in served if k != "checksums"}}
         ref = reference_configs_subprocess(["stamp"])
+        progress("reference stamp done")
         configs["1_stamp"]["reference"] = ref.get("stamp", ref.get("unavailable"))
         configs["3_large"]["reference"] = REFERENCE_LARGE_UNAVAILABLE
         configs["5_served"]["reference"] = ("n/a: the reference's queue (data_structs/queue.cuh) does not "
@@ -691,6 +712,7 @@ def main():
     }
     if world == 1 and not args.no_cpu_baseline:
         base, glibc = cpu_baseline(N, R)
+        progress("cpu baseline done")
         line["cpu_baseline"] = base
         line["host_malloc_baseline"] = glibc
     print(json.dumps(line))
