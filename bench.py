@@ -35,6 +35,7 @@ Multi-GPU: replicas only (each rank its own allocator; no collective on the
 data path); `value` sums all ranks' ops over the slowest rank's time.
 """
 import argparse
+import faulthandler
 import json
 import os
 import subprocess
@@ -61,7 +62,7 @@ WORKLOAD = ("mixed-size churn: arena 128 GiB as 2,048 segments of 64 MiB (Gallat
 TUNED = dict(pinned_slots_first=0, pinned_slots_min=0, gather_unlocked_below=16,
              bytes_per_segment=SEGMENT, spare_blocks=1, block_layout=1)
 # gal_bench_churn modes: bit 0 CTA claim, bit 2 cached pinned blocks, bit 3 allocator-only,
-# bit 7 the cached form at 4 CTAs of 256 threads per SM
+# bits 7 / 8 the plain or cached malloc kernel compiled for 4 / 3 CTAs of 256 threads per SM
 FORMS = {"plain": 0, "cta": 1, "cached": 4}
 SERVER_STREAMS = [          # (requests, lo, hi, log-uniform, kept for this many later requests)
     (6_000_000, 16, 128, 0, 1),
@@ -91,8 +92,10 @@ def parse():
     p.add_argument("--malloc-form", default="cached", choices=["cached", "cta", "plain"],
                    help="headline malloc: persistent CTAs with cached pinned blocks, one CTA claim per "
                         "class, or one thread per request")
-    p.add_argument("--ctas-per-sm", type=int, default=4, choices=[2, 4],
-                   help="cached form: resident CTAs of 256 threads per SM")
+    p.add_argument("--ctas-per-sm", type=int, default=4, choices=[0, 3, 4],
+                   help="plain and cached forms: CTAs of 256 threads per SM the malloc kernel's "
+                        "registers must allow (0: the kernel's own count -- no bound for plain, 2 "
+                        "for cached)")
     p.add_argument("--slots", type=int, default=0,
                    help="pinned slots per class (0: one per SM); small profiling cases use fewer")
     p.add_argument("--block-layout", default="record", choices=["record", "dense"],
@@ -341,7 +344,7 @@ def reference_configs_subprocess(only):
     """reference_configs in a child process; {} when it cannot run."""
     try:
         r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--configs", "--impl", "reference",
-                            "--only", ",".join(only)], capture_output=True, text=True, timeout=900)
+                            "--only", ",".join(only)], capture_output=True, text=True, timeout=300)
         for line in reversed(r.stdout.splitlines()):
             if line.startswith("{"):
                 return json.loads(line)
@@ -467,6 +470,8 @@ def churn_ok(res):
 
 def main():
     args = parse()
+    # a phase that runs far longer than its usual seconds shows where it waits
+    faulthandler.dump_traceback_later(240, repeat=True, file=sys.stderr)
     world, rank, local = dist_setup(args)
     if args.configs:
         if args.impl == "ours":
@@ -488,8 +493,8 @@ def main():
     arena = args.arena_gib << 30
     TUNED["block_layout"] = 1 if args.block_layout == "record" else 0
     TUNED["pinned_slots_first"] = TUNED["pinned_slots_min"] = args.slots
-    occ_bit = 128 if args.ctas_per_sm == 4 else 0
-    form_mode = {"cached": FORMS["cached"] | occ_bit, "cta": FORMS["cta"], "plain": FORMS["plain"]}
+    occ_bit = {0: 0, 3: 256, 4: 128}[args.ctas_per_sm]
+    form_mode = {"cached": FORMS["cached"] | occ_bit, "cta": FORMS["cta"], "plain": FORMS["plain"] | occ_bit}
     head_mode = form_mode[args.malloc_form]
     g = G.Gallatin.generate_on_device(arena, ALLOC_SEED, **TUNED)
 
@@ -600,7 +605,7 @@ def main():
     # every malloc form at the same knobs, full churn and allocator-only churn
     steps_f = max(3, args.steps // 3)
     forms = {}
-    for name, mode in (("plain", 0), ("cta", FORMS["cta"]), ("cached", FORMS["cached"] | occ_bit)):
+    for name, mode in (("plain", form_mode["plain"]), ("cta", form_mode["cta"]), ("cached", form_mode["cached"])):
         entry = {}
         for bare, key in ((0, "full"), (8, "allocator_only")):
             gf = G.Gallatin.generate_on_device(arena, ALLOC_SEED, **TUNED)

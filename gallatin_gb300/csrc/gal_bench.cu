@@ -55,9 +55,13 @@ namespace {
 
 constexpr int BT = 512;  // batched CTA size
 
-template <bool PAYLOAD>
-__global__ void k_churn_malloc_plain(const gal::state *s, void **ptrs, uint32_t *live, uint64_t base,
-                                     uint64_t n, uint32_t seed, unsigned long long *stats) {
+// one thread per request; MINB: CTAs of 256 threads per SM its registers must
+// allow (1: no bound, 94 registers; 3: 85; 4: 64)
+constexpr int PLAIN_BT = 256;
+template <bool PAYLOAD, int MINB>
+__global__ void __launch_bounds__(PLAIN_BT, MINB)
+    k_churn_malloc_plain(const gal::state *s, void **ptrs, uint32_t *live, uint64_t base,
+                         uint64_t n, uint32_t seed, unsigned long long *stats) {
   plain_alloc a{s, nullptr};
   galwl::churn_malloc_body<plain_alloc, PAYLOAD>(&a, ptrs, live, base, n, seed, stats);
 }
@@ -367,7 +371,7 @@ struct churn_ctx {
   uint32_t R, seed;
   int batched;
   bool payload;   // false: the allocator-only form (no payload written or checked)
-  int minb;       // cached malloc: CTAs per SM its registers allow (2 or 4)
+  int minb;       // CTAs per SM the malloc kernel's registers allow (2: the default; 3 or 4)
   int grid_c;     // persistent grid of the cached malloc
   size_t stage_bytes;  // dynamic shared memory of the free phase: staged segment classes (0: none)
   void **ptrs;
@@ -422,17 +426,13 @@ void enqueue_step(churn_ctx &c, cudaStream_t st, bool capturing) {
     mark(0, true);
     if (c.batched & 4) {
       const unsigned gc = (unsigned)std::min<uint64_t>((c.N + CACHED_BT - 1) / CACHED_BT, (uint64_t)c.grid_c);
-      if (c.minb == 4) {
-        if (c.payload)
-          k_churn_malloc_cached<true, 4><<<gc, CACHED_BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats);
-        else
-          k_churn_malloc_cached<false, 4><<<gc, CACHED_BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats);
-      } else {
-        if (c.payload)
-          k_churn_malloc_cached<true, 2><<<gc, CACHED_BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats);
-        else
-          k_churn_malloc_cached<false, 2><<<gc, CACHED_BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats);
-      }
+      auto launch = [&](auto kern) { kern<<<gc, CACHED_BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats); };
+      if (c.minb == 4)
+        c.payload ? launch(k_churn_malloc_cached<true, 4>) : launch(k_churn_malloc_cached<false, 4>);
+      else if (c.minb == 3)
+        c.payload ? launch(k_churn_malloc_cached<true, 3>) : launch(k_churn_malloc_cached<false, 3>);
+      else
+        c.payload ? launch(k_churn_malloc_cached<true, 2>) : launch(k_churn_malloc_cached<false, 2>);
     } else if (c.batched & 1) {
       const int per = 1 << c.k_shift;  // requests per thread per iteration
       unsigned gk = (unsigned)std::min<uint64_t>((c.N + (uint64_t)BW * per - 1) / ((uint64_t)BW * per),
@@ -443,12 +443,15 @@ void enqueue_step(churn_ctx &c, cudaStream_t st, bool capturing) {
         k_churn_malloc_batched<2><<<gk, BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats);
       else
         k_churn_malloc_batched<1><<<gk, BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats);
-    } else if (c.payload) {
-      k_churn_malloc_plain<true><<<(unsigned)((c.N + 255) / 256), 256, 0, st>>>(c.d, c.ptrs, c.live, base,
-                                                                              c.N, c.seed, c.stats);
     } else {
-      k_churn_malloc_plain<false><<<(unsigned)((c.N + 255) / 256), 256, 0, st>>>(c.d, c.ptrs, c.live, base,
-                                                                               c.N, c.seed, c.stats);
+      const unsigned gp = (unsigned)((c.N + PLAIN_BT - 1) / PLAIN_BT);
+      auto launch = [&](auto kern) { kern<<<gp, PLAIN_BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats); };
+      if (c.minb == 4)
+        c.payload ? launch(k_churn_malloc_plain<true, 4>) : launch(k_churn_malloc_plain<false, 4>);
+      else if (c.minb == 3)
+        c.payload ? launch(k_churn_malloc_plain<true, 3>) : launch(k_churn_malloc_plain<false, 3>);
+      else
+        c.payload ? launch(k_churn_malloc_plain<true, 1>) : launch(k_churn_malloc_plain<false, 1>);
     }
     mark(0, false);
   }
@@ -478,9 +481,11 @@ extern "C" {
  * form (no payload written or checked), bits 4-5: log2 of the requests each
  * thread of the CTA-aggregated malloc serves per iteration (0-2), bit 6: the
  * free phase looks segment classes up in global memory instead of a copy
- * staged in shared memory, bit 7: the cached malloc at 4 CTAs of 256 threads
- * per SM (64 registers) instead of 2; use_graph: the step is one captured
- * CUDA graph.
+ * staged in shared memory, bit 7: the cached or per-thread malloc kernel
+ * compiled for 4 CTAs of 256 threads per SM (64 registers), bit 8: for 3 CTAs
+ * (85 registers) -- without either, the cached kernel is compiled for 2 and
+ * the per-thread kernel has no register bound; use_graph: the step is one
+ * captured CUDA graph.
  * step_ms[i]: duration of timed step i (CUDA events on the launching stream). */
 int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, uint32_t seed,
                     int batched, int use_graph, int warmup, int steps, float *step_ms,
@@ -496,7 +501,7 @@ int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, 
   c.seed = seed;
   c.batched = batched & 7;
   c.payload = !(batched & 8);
-  c.minb = (batched & 128) ? 4 : 2;
+  c.minb = (batched & 128) ? 4 : (batched & 256) ? 3 : 2;
   c.k_shift = (batched >> 4) & 3;
   if (c.k_shift > 2) return GAL_ERR_ARGS;
   c.ptrs = nullptr;
@@ -524,6 +529,8 @@ int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, 
   per_sm = 0;
   if (c.minb == 4)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_churn_malloc_cached<true, 4>, CACHED_BT, 0);
+  else if (c.minb == 3)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_churn_malloc_cached<true, 3>, CACHED_BT, 0);
   else
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_churn_malloc_cached<true, 2>, CACHED_BT, 0);
   c.grid_c = sms * (per_sm > 0 ? per_sm : 1);
