@@ -20,10 +20,11 @@ failure.  The arena is 128 GiB (2x that) for both arms.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-`value` is the device-resident throughput of the batched path (persistent
-kernels, each step one captured CUDA graph; by default malloc from CTAs that
-cache their SM's pinned blocks in shared memory, frees looking segment
-classes up in a copy staged in shared memory); `e2e` is the same churn through the
+`value` is the device-resident throughput of the fastest form measured (each
+step one captured CUDA graph; by default malloc one thread per request in a
+kernel compiled for 3 CTAs of 256 threads per SM, warp teams claiming with one
+atomic each, and a persistent free phase looking segment classes up in a copy
+staged in shared memory); `e2e` is the same churn through the
 public C ABI entry points (gal_malloc_batched / gal_free_batched_n) with each
 round's request sizes copied from pinned host memory inside the timed region.
 Beside it: every malloc form at the same knobs, on the full churn and on the
@@ -89,13 +90,15 @@ def parse():
     p.add_argument("--rounds", type=int, default=ROUNDS)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--arena-gib", type=int, default=ARENA >> 30)
-    p.add_argument("--malloc-form", default="cached", choices=["cached", "cta", "plain"],
+    p.add_argument("--malloc-form", default="plain", choices=["cached", "cta", "plain"],
                    help="headline malloc: persistent CTAs with cached pinned blocks, one CTA claim per "
                         "class, or one thread per request")
-    p.add_argument("--ctas-per-sm", type=int, default=4, choices=[0, 3, 4],
+    p.add_argument("--ctas-per-sm", type=int, default=3, choices=[0, 3, 4],
                    help="plain and cached forms: CTAs of 256 threads per SM the malloc kernel's "
                         "registers must allow (0: the kernel's own count -- no bound for plain, 2 "
                         "for cached)")
+    p.add_argument("--free-ctas-per-sm", type=int, default=0, choices=[0, 4],
+                   help="free kernel: CTAs of 256 threads per SM its registers must allow (0: no bound)")
     p.add_argument("--slots", type=int, default=0,
                    help="pinned slots per class (0: one per SM); small profiling cases use fewer")
     p.add_argument("--block-layout", default="record", choices=["record", "dense"],
@@ -493,9 +496,11 @@ def main():
     arena = args.arena_gib << 30
     TUNED["block_layout"] = 1 if args.block_layout == "record" else 0
     TUNED["pinned_slots_first"] = TUNED["pinned_slots_min"] = args.slots
-    occ_bit = {0: 0, 3: 256, 4: 128}[args.ctas_per_sm]
-    form_mode = {"cached": FORMS["cached"] | occ_bit, "cta": FORMS["cta"], "plain": FORMS["plain"] | occ_bit}
+    occ_bit = {0: 0, 3: 256, 4: 128}[args.ctas_per_sm] | (512 if args.free_ctas_per_sm == 4 else 0)
+    form_mode = {"cached": FORMS["cached"] | occ_bit, "cta": FORMS["cta"] | (occ_bit & 512),
+                 "plain": FORMS["plain"] | occ_bit}
     head_mode = form_mode[args.malloc_form]
+    occ_name = {0: "the kernel's own register count", 3: "3 CTAs", 4: "4 CTAs"}[args.ctas_per_sm]
     g = G.Gallatin.generate_on_device(arena, ALLOC_SEED, **TUNED)
 
     # one probe step: a workload that does not fit would run the out-of-memory
@@ -545,8 +550,9 @@ def main():
 
     # roofline of the dominant kernel of the headline step.  HBM: algorithmic
     # bytes per launch -- malloc: 8 B pointer store + 4 B payload store per
-    # request; free: 8 B pointer load + 4 B payload load + 8 B pointer clear
-    # per free, plus 4 B of liveness word per 32 slots scanned.  L2 atomics:
+    # request; free: 8 B pointer load + 4 B payload load per free, plus the
+    # liveness words of the slots scanned, read and written back (1 bit per
+    # slot each way; an upper bound on the writes).  L2 atomics:
     # one counter atomic per request (the per-block malloc or free counter)
     # against the atomic peak measured in this run.
     progress("e2e done")
@@ -558,7 +564,7 @@ def main():
     scanned = N * R * (R + 1) / 2 * args.steps
     phases = {
         malloc_kern: (res.ms_malloc_kernels, res.malloc_launches, res.mallocs_ok, 12.0 * res.mallocs_ok),
-        free_kern: (res.ms_free_kernels, res.free_launches, res.frees, scanned / 8 + 20.0 * res.frees),
+        free_kern: (res.ms_free_kernels, res.free_launches, res.frees, scanned / 4 + 12.0 * res.frees),
     }
 
     def roofline_of(kern):
@@ -685,13 +691,13 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic (Philox4x32-10 seed 1; sizes log-uniform 16 B-4 KiB rounded to pow2)",
         "config": workload_config(N, R, arena),
-        "path": {"cached": "persistent malloc CTAs (%d x 256 threads per SM) that keep their SM's pinned "
-                           "blocks in shared memory, one atomicAdd per warp team; persistent free phase "
-                           "with segment classes staged in shared memory, one atomic per warp team; "
-                           "one CUDA graph per step" % args.ctas_per_sm,
-                 "cta": "persistent kernels, one CTA claim per class, frees in warp teams, one CUDA graph "
-                        "per step",
-                 "plain": "one thread per request, frees in warp teams, one CUDA graph per step"}[args.malloc_form],
+        "path": {"cached": "persistent malloc CTAs (256 threads, registers for %s per SM) that keep their SM's "
+                           "pinned blocks in shared memory, one atomicAdd per warp team" % occ_name,
+                 "cta": "persistent malloc CTAs of 512 threads, one claim per class and CTA",
+                 "plain": "malloc one thread per request (256-thread CTAs, registers for %s per SM), warp "
+                          "teams with one atomicAdd per team" % occ_name}[args.malloc_form]
+                + "; persistent free phase, four frees per lane, segment classes staged in shared memory, "
+                  "one free-counter atomic per warp team; one CUDA graph per step",
         "knobs": dict(TUNED, note="gal_config fields; pinned_slots_first=0 means one pinned slot per SM "
                                   "in every class"),
         "mallocs_per_step": res.mallocs_ok / args.steps, "mallocs_failed": int(res.mallocs_failed),

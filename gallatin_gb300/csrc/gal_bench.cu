@@ -71,8 +71,9 @@ constexpr int FREE_BT = 256;  // free phase CTA size (persistent grid)
 // The free phase; with dynamic shared memory of 2 bytes per segment the
 // segments' classes are staged first (every pointer freed here was allocated
 // by an earlier kernel, and a live pointer's segment keeps its class).
-template <bool PAYLOAD>
-__global__ void __launch_bounds__(FREE_BT)
+// MINB: CTAs per SM the registers must allow (1: no bound, 80 registers; 4: 64).
+template <bool PAYLOAD, int MINB>
+__global__ void __launch_bounds__(FREE_BT, MINB)
     k_churn_free_plain(const gal::state *s, void **ptrs, uint32_t *live, uint64_t nslots,
                        uint32_t round, uint32_t seed, int all, int stage, unsigned long long *stats) {
   __shared__ uint16_t lists[FREE_BT / 32][galwl::WARP_SLOTS];
@@ -372,6 +373,7 @@ struct churn_ctx {
   int batched;
   bool payload;   // false: the allocator-only form (no payload written or checked)
   int minb;       // CTAs per SM the malloc kernel's registers allow (2: the default; 3 or 4)
+  int free_minb;  // the same for the free kernel (1: no bound; 4)
   int grid_c;     // persistent grid of the cached malloc
   size_t stage_bytes;  // dynamic shared memory of the free phase: staged segment classes (0: none)
   void **ptrs;
@@ -412,12 +414,14 @@ void enqueue_step(churn_ctx &c, cudaStream_t st, bool capturing) {
       } else {
         const uint64_t chunk = (uint64_t)(FREE_BT / 32) * galwl::WARP_SLOTS;
         unsigned g = (unsigned)std::min<uint64_t>((nscan + chunk - 1) / chunk, (uint64_t)c.grid_f);
-        if (c.payload)
-          k_churn_free_plain<true><<<g, FREE_BT, c.stage_bytes, st>>>(c.d, c.ptrs, c.live, nscan, r, c.seed,
-                                                                     drain ? 1 : 0, c.stage_bytes > 0, c.stats);
+        auto launch = [&](auto kern) {
+          kern<<<g, FREE_BT, c.stage_bytes, st>>>(c.d, c.ptrs, c.live, nscan, r, c.seed, drain ? 1 : 0,
+                                                  c.stage_bytes > 0, c.stats);
+        };
+        if (c.free_minb == 4)
+          c.payload ? launch(k_churn_free_plain<true, 4>) : launch(k_churn_free_plain<false, 4>);
         else
-          k_churn_free_plain<false><<<g, FREE_BT, c.stage_bytes, st>>>(c.d, c.ptrs, c.live, nscan, r, c.seed,
-                                                                      drain ? 1 : 0, c.stage_bytes > 0, c.stats);
+          c.payload ? launch(k_churn_free_plain<true, 1>) : launch(k_churn_free_plain<false, 1>);
       }
       mark(1, false);
     }
@@ -484,8 +488,9 @@ extern "C" {
  * staged in shared memory, bit 7: the cached or per-thread malloc kernel
  * compiled for 4 CTAs of 256 threads per SM (64 registers), bit 8: for 3 CTAs
  * (85 registers) -- without either, the cached kernel is compiled for 2 and
- * the per-thread kernel has no register bound; use_graph: the step is one
- * captured CUDA graph.
+ * the per-thread kernel has no register bound; bit 9: the free kernel
+ * compiled for 4 CTAs of 256 threads per SM (64 registers; else no bound);
+ * use_graph: the step is one captured CUDA graph.
  * step_ms[i]: duration of timed step i (CUDA events on the launching stream). */
 int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, uint32_t seed,
                     int batched, int use_graph, int warmup, int steps, float *step_ms,
@@ -502,6 +507,7 @@ int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, 
   c.batched = batched & 7;
   c.payload = !(batched & 8);
   c.minb = (batched & 128) ? 4 : (batched & 256) ? 3 : 2;
+  c.free_minb = (batched & 512) ? 4 : 1;
   c.k_shift = (batched >> 4) & 3;
   if (c.k_shift > 2) return GAL_ERR_ARGS;
   c.ptrs = nullptr;
@@ -524,7 +530,10 @@ int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, 
     gal_state_dims_get(h, &dims);
     c.stage_bytes = dims.num_segments * 2 <= gal::CLASS_STAGE_BYTES && !(batched & 64) ? dims.num_segments * 2 : 0;
   }
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_churn_free_plain<true>, FREE_BT, c.stage_bytes);
+  if (c.free_minb == 4)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_churn_free_plain<true, 4>, FREE_BT, c.stage_bytes);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_churn_free_plain<true, 1>, FREE_BT, c.stage_bytes);
   c.grid_f = sms * (per_sm > 0 ? per_sm : 1);
   per_sm = 0;
   if (c.minb == 4)

@@ -27,7 +27,7 @@ struct gal_handle {
   char *arena = nullptr;
   uint64_t arena_bytes = 0;
   gal_state_dims dims{};
-  int grid_malloc = 0, grid_free = 0;  // persistent grids of the batched kernels (0: not yet known)
+  int grid_free = 0;  // persistent grid of the batched free kernel (0: not yet known)
 };
 
 namespace {
@@ -236,20 +236,19 @@ __global__ void k_free_per_thread(const gal::state *s, void *const *ptrs, uint64
 
 constexpr int BATCH_THREADS = 512;
 
-// Batched malloc: a persistent grid of CTAs that each serve many requests per
-// thread, claiming through gal::malloc_cached: warp teams take the SM's
-// pinned block from the CTA's copy in shared memory and go to the pinned
-// slot in global memory only when the copy has gone stale.
+// Batched malloc: one thread per request, warp teams claiming with one
+// atomicAdd per team on their SM's pinned block (gal::malloc), compiled for
+// four CTAs of 256 threads per SM (64 registers).  On the mixed 16 B-4 KiB
+// churn's requests this served 64 Mi mallocs in 2.2 ms per step, against
+// 2.6 ms for the same kernel without a register bound and for a persistent
+// grid keeping the pinned blocks in shared memory (gal::malloc_cached).
 constexpr int MALLOC_THREADS = 256;
 
-__global__ void __launch_bounds__(MALLOC_THREADS)
+__global__ void __launch_bounds__(MALLOC_THREADS, 4)
     k_malloc_batched(const gal::state *s, const uint64_t *sizes, uint64_t n, void **out) {
-  __shared__ gal::slot_cache cache;
-  gal::slot_cache_init(cache);
-  __syncthreads();
   for (uint64_t i = (uint64_t)blockIdx.x * MALLOC_THREADS + threadIdx.x; i < n;
        i += (uint64_t)gridDim.x * MALLOC_THREADS)
-    out[i] = gal::malloc_cached(s, sizes[i], cache);
+    out[i] = gal::malloc(s, sizes[i]);
 }
 
 // Batched free: each thread takes FREE_PER_THREAD entries per pass of a
@@ -824,10 +823,8 @@ int gal_trim(gal_handle *h, void *stream) {
 int gal_malloc_batched(gal_handle *h, const uint64_t *sizes, uint64_t n, void **out, void *stream) {
   if (!h || (n && (!sizes || !out))) return GAL_ERR_ARGS;
   if (!n) return GAL_OK;
-  unsigned g = grid_for(n, MALLOC_THREADS);
-  if (!h->grid_malloc) h->grid_malloc = persistent_grid(h->device, k_malloc_batched, MALLOC_THREADS);
-  unsigned p = (unsigned)h->grid_malloc;
-  k_malloc_batched<<<g < p ? g : p, MALLOC_THREADS, 0, (cudaStream_t)stream>>>(h->d_state, sizes, n, out);
+  k_malloc_batched<<<grid_for(n, MALLOC_THREADS), MALLOC_THREADS, 0, (cudaStream_t)stream>>>(h->d_state, sizes,
+                                                                                          n, out);
   CUDA_TRY(cudaGetLastError());
   return GAL_OK;
 }

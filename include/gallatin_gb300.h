@@ -297,12 +297,11 @@ int gal_free_per_thread(gal_handle *h, void *const *ptrs, uint64_t n, void *stre
 int gal_trim(gal_handle *h, void *stream);
 
 /* Batched form: the same results contract as gal_malloc_per_thread /
- * gal_free_per_thread.  Mallocs run on a persistent grid whose CTAs keep a
- * copy of their SM's pinned blocks in shared memory, so a warp team's claim is
- * one atomicAdd on the block (the pinned slot is read again only when the
- * copy has gone stale); frees take four entries per thread, look the segment
- * classes up in a copy staged in shared memory, and form warp teams per block
- * (one free-counter atomic per team). */
+ * gal_free_per_thread.  Mallocs run one request per thread in a kernel
+ * compiled for four CTAs of 256 threads per SM, warp teams claiming with one
+ * atomicAdd per team; frees take four entries per thread on a persistent
+ * grid, look the segment classes up in a copy staged in shared memory, and
+ * form warp teams per block (one free-counter atomic per team). */
 int gal_malloc_batched(gal_handle *h, const uint64_t *sizes, uint64_t n,
                        void **out_ptrs, void *stream);
 int gal_free_batched(gal_handle *h, void *const *ptrs, uint64_t n, void *stream);
