@@ -97,7 +97,9 @@ def parse():
                    help="plain and cached forms: CTAs of 256 threads per SM the malloc kernel's "
                         "registers must allow (0: the kernel's own count -- no bound for plain, 2 "
                         "for cached)")
-    p.add_argument("--free-ctas-per-sm", type=int, default=0, choices=[0, 4],
+    p.add_argument("--per-thread", type=int, default=1, choices=[1, 2, 4],
+                   help="plain form: requests each lane serves through gal::malloc_n")
+    p.add_argument("--free-ctas-per-sm", type=int, default=4, choices=[0, 4],
                    help="free kernel: CTAs of 256 threads per SM its registers must allow (0: no bound)")
     p.add_argument("--slots", type=int, default=0,
                    help="pinned slots per class (0: one per SM); small profiling cases use fewer")
@@ -497,7 +499,8 @@ def main():
     TUNED["block_layout"] = 1 if args.block_layout == "record" else 0
     TUNED["pinned_slots_first"] = TUNED["pinned_slots_min"] = args.slots
     occ_bit = {0: 0, 3: 256, 4: 128}[args.ctas_per_sm] | (512 if args.free_ctas_per_sm == 4 else 0)
-    form_mode = {"cached": FORMS["cached"] | occ_bit, "cta": FORMS["cta"] | (occ_bit & 512),
+    occ_bit |= {1: 0, 2: 1 << 11, 4: 2 << 11}[args.per_thread]
+    form_mode = {"cached": FORMS["cached"] | (occ_bit & 0x3FF), "cta": FORMS["cta"] | (occ_bit & 512),
                  "plain": FORMS["plain"] | occ_bit}
     head_mode = form_mode[args.malloc_form]
     occ_name = {0: "the kernel's own register count", 3: "3 CTAs", 4: "4 CTAs"}[args.ctas_per_sm]
@@ -666,6 +669,16 @@ def main():
             progress(f"server {key} done")
         server["streams"] = [list(s) for s in SERVER_STREAMS]
 
+    # hot-word layout: L2 atomics/s on 8-byte counters, each hit by warps of
+    # its own, packed 1, 2 or 4 to a 32-byte sector (304 counters: two per SM,
+    # as the pinned blocks of two classes; 1,216: eight per SM)
+    hot_words = {}
+    if world == 1:
+        for hot in (304, 1216):
+            hot_words[str(hot)] = {str(k): G.sector_probe(hot, k) / 1e9 for k in (1, 2, 4)}
+        hot_words["unit"] = "Gatomic/s by counters per 32-byte sector"
+        progress("hot-word probe done")
+
     # secondary workloads, ours and the reference build's
     configs = {}
     if world == 1 and not args.no_extras:
@@ -717,6 +730,7 @@ def main():
                         "CUDA graph (three streams)"},
         "latency": latency,
         "server": server,
+        "hot_word_probe": hot_words,
         "configs_secondary": configs,
         "gpu_launches": int(res.malloc_launches + res.free_launches),
         "clocks": clk.summary(),

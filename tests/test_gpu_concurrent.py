@@ -386,6 +386,30 @@ def test_cached_block_churn_payloads_and_fresh_trees(G, mode):
         g.close()
 
 
+@pytest.mark.parametrize("mode", [256, 128 | 512, 256 | 512 | (1 << 11), 128 | (1 << 11),
+                                  (2 << 11) | 512, 8 | 256 | 512 | (1 << 11)])
+def test_per_thread_churn_forms_payloads_and_fresh_trees(G, mode):
+    """The per-thread malloc kernel compiled for 3 or 4 CTAs per SM, lanes
+    serving 1, 2 or 4 requests each through gal::malloc_n, and the free
+    kernel compiled for 4 CTAs per SM: every malloc served, payloads intact,
+    frees balance the mallocs, and after trim the trees are fresh again."""
+    g = G.Gallatin.generate_on_device(32 << 30, 42, spare_blocks=1, pinned_slots_first=0,
+                                      bytes_per_segment=64 << 20, gather_unlocked_below=16)
+    try:
+        fresh = g.export()
+        N, R = 1 << 19, 6
+        ms, r = g.bench_churn(N, R, 1, mode, True, 1, 2)
+        assert r.mallocs_ok == 2 * N * R and r.mallocs_failed == 0
+        assert r.payload_mismatch == 0
+        assert r.frees == r.mallocs_ok
+        assert r.error_word == 0
+        g.trim()
+        assert g.error_word() == 0, g.error_info()
+        assert g.export().diff(fresh, fields=TREE_FIELDS) == []
+    finally:
+        g.close()
+
+
 @pytest.mark.parametrize("layout", [0, 1])
 def test_block_layouts_serve_the_same_churn(G, layout):
     """Dense counter arrays and one 32-byte record per block: the same churn,
