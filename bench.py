@@ -97,8 +97,6 @@ def parse():
                    help="plain and cached forms: CTAs of 256 threads per SM the malloc kernel's "
                         "registers must allow (0: the kernel's own count -- no bound for plain, 2 "
                         "for cached)")
-    p.add_argument("--per-thread", type=int, default=1, choices=[1, 2, 4],
-                   help="plain form: requests each lane serves through gal::malloc_n")
     p.add_argument("--free-ctas-per-sm", type=int, default=4, choices=[0, 4],
                    help="free kernel: CTAs of 256 threads per SM its registers must allow (0: no bound)")
     p.add_argument("--slots", type=int, default=0,
@@ -106,6 +104,8 @@ def parse():
     p.add_argument("--block-layout", default="record", choices=["record", "dense"],
                    help="block counters: one 32-byte record per block, or dense arrays")
     p.add_argument("--quick", action="store_true", help="headline steps only (profiling)")
+    p.add_argument("--quick-e2e", action="store_true",
+                   help="headline steps, then the end-to-end C-ABI steps only (profiling)")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the secondary workloads and the reference figures beside them")
     p.add_argument("--configs", action="store_true",
@@ -499,8 +499,7 @@ def main():
     TUNED["block_layout"] = 1 if args.block_layout == "record" else 0
     TUNED["pinned_slots_first"] = TUNED["pinned_slots_min"] = args.slots
     occ_bit = {0: 0, 3: 256, 4: 128}[args.ctas_per_sm] | (512 if args.free_ctas_per_sm == 4 else 0)
-    occ_bit |= {1: 0, 2: 1 << 11, 4: 2 << 11}[args.per_thread]
-    form_mode = {"cached": FORMS["cached"] | (occ_bit & 0x3FF), "cta": FORMS["cta"] | (occ_bit & 512),
+    form_mode = {"cached": FORMS["cached"] | occ_bit, "cta": FORMS["cta"] | (occ_bit & 512),
                  "plain": FORMS["plain"] | occ_bit}
     head_mode = form_mode[args.malloc_form]
     occ_name = {0: "the kernel's own register count", 3: "3 CTAs", 4: "4 CTAs"}[args.ctas_per_sm]
@@ -550,6 +549,12 @@ def main():
     errors = g.error_word() | eres.error_word
     if eres.mallocs_failed or eres.payload_mismatch:
         errors |= 1 << 31
+    if args.quick_e2e:
+        g.close()
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "e2e": e2e_v, "quick": True,
+                              "result": res.as_dict(), "e2e_result": eres.as_dict()}))
+        return
 
     # roofline of the dominant kernel of the headline step.  HBM: algorithmic
     # bytes per launch -- malloc: 8 B pointer store + 4 B payload store per

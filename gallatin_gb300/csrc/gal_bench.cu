@@ -66,35 +66,6 @@ __global__ void __launch_bounds__(PLAIN_BT, MINB)
   galwl::churn_malloc_body<plain_alloc, PAYLOAD>(&a, ptrs, live, base, n, seed, stats);
 }
 
-// K requests per lane through gal::malloc_n: warp w serves the 32 K slots
-// from w * 32 K on, lane l's request k being slot + 32 k + l, so each k covers
-// one liveness word.  Whole warps: n is a multiple of SLOT_ALIGN (128), which
-// 32 K divides for K <= 4.
-template <bool PAYLOAD, int MINB, int K>
-__global__ void __launch_bounds__(PLAIN_BT, MINB)
-    k_churn_malloc_multi(const gal::state *s, void **ptrs, uint32_t *live, uint64_t base,
-                         uint64_t n, uint32_t seed, unsigned long long *stats) {
-  const uint64_t first = (((uint64_t)blockIdx.x * PLAIN_BT + threadIdx.x) >> 5) * 32u * K;
-  if (first >= n) return;  // warp-uniform
-  const uint32_t lane = threadIdx.x & 31u;
-  uint64_t size[K];
-  void *p[K];
-#pragma unroll
-  for (int k = 0; k < K; k++) size[k] = galwl::mixed_size(base + first + 32u * k + lane, seed);
-  gal::malloc_n<K>(s, size, p, 0xFFFFFFFFu);
-  uint32_t ok = 0;
-#pragma unroll
-  for (int k = 0; k < K; k++) {
-    const uint64_t slot = base + first + 32u * k + lane;
-    if (PAYLOAD && p[k]) *(volatile uint32_t *)p[k] = galwl::payload(slot, seed);
-    ptrs[slot] = p[k];
-    galwl::publish_live(live, slot, p[k] != nullptr);
-    ok += p[k] != nullptr;
-  }
-  galwl::warp_add(stats, 0, ok);
-  galwl::warp_add(stats, 1, K - ok);
-}
-
 constexpr int FREE_BT = 256;  // free phase CTA size (persistent grid)
 
 // The free phase; with dynamic shared memory of 2 bytes per segment the
@@ -403,7 +374,6 @@ struct churn_ctx {
   bool payload;   // false: the allocator-only form (no payload written or checked)
   int minb;       // CTAs per SM the malloc kernel's registers allow (2: the default; 3 or 4)
   int free_minb;  // the same for the free kernel (1: no bound; 4)
-  int per_thread; // per-thread malloc form: requests per lane (1, 2 or 4; gal::malloc_n)
   int grid_c;     // persistent grid of the cached malloc
   size_t stage_bytes;  // dynamic shared memory of the free phase: staged segment classes (0: none)
   void **ptrs;
@@ -477,17 +447,6 @@ void enqueue_step(churn_ctx &c, cudaStream_t st, bool capturing) {
         k_churn_malloc_batched<2><<<gk, BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats);
       else
         k_churn_malloc_batched<1><<<gk, BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats);
-    } else if (c.per_thread > 1) {
-      const unsigned gp = (unsigned)((c.N + (uint64_t)PLAIN_BT * c.per_thread - 1) / ((uint64_t)PLAIN_BT * c.per_thread));
-      auto launch = [&](auto kern) { kern<<<gp, PLAIN_BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats); };
-      if (c.per_thread == 4)
-        c.payload ? launch(k_churn_malloc_multi<true, 1, 4>) : launch(k_churn_malloc_multi<false, 1, 4>);
-      else if (c.minb == 4)
-        c.payload ? launch(k_churn_malloc_multi<true, 4, 2>) : launch(k_churn_malloc_multi<false, 4, 2>);
-      else if (c.minb == 3)
-        c.payload ? launch(k_churn_malloc_multi<true, 3, 2>) : launch(k_churn_malloc_multi<false, 3, 2>);
-      else
-        c.payload ? launch(k_churn_malloc_multi<true, 1, 2>) : launch(k_churn_malloc_multi<false, 1, 2>);
     } else {
       const unsigned gp = (unsigned)((c.N + PLAIN_BT - 1) / PLAIN_BT);
       auto launch = [&](auto kern) { kern<<<gp, PLAIN_BT, 0, st>>>(c.d, c.ptrs, c.live, base, c.N, c.seed, c.stats); };
@@ -531,8 +490,7 @@ extern "C" {
  * (85 registers) -- without either, the cached kernel is compiled for 2 and
  * the per-thread kernel has no register bound; bit 9: the free kernel
  * compiled for 4 CTAs of 256 threads per SM (64 registers; else no bound);
- * bits 11-12: log2 of the requests each lane of the per-thread malloc serves
- * through gal::malloc_n (0-2; at 4 the kernel has no register bound);
+ * higher bits are refused;
  * use_graph: the step is one captured CUDA graph.
  * step_ms[i]: duration of timed step i (CUDA events on the launching stream). */
 int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, uint32_t seed,
@@ -551,8 +509,7 @@ int gal_bench_churn(gal_handle *h, uint64_t threads_per_round, uint32_t rounds, 
   c.payload = !(batched & 8);
   c.minb = (batched & 128) ? 4 : (batched & 256) ? 3 : 2;
   c.free_minb = (batched & 512) ? 4 : 1;
-  c.per_thread = 1 << ((batched >> 11) & 3);
-  if (c.per_thread > 4) return GAL_ERR_ARGS;
+  if (batched & ~0x3FF) return GAL_ERR_ARGS;
   c.k_shift = (batched >> 4) & 3;
   if (c.k_shift > 2) return GAL_ERR_ARGS;
   c.ptrs = nullptr;

@@ -1063,97 +1063,6 @@ GAL_DEVICE_INLINE void *malloc_team(const state *s, uint64_t size, uint32_t call
   return malloc_from<true>(s, size, callers);
 }
 
-// N requests per lane, served as N calls of malloc_team(s, size[k], callers)
-// would be, but with the pinned-slot reads of all N issued back to back and
-// then their claim atomics back to back, so the round trips of the N claims
-// overlap instead of following one another.  Every lane of `callers` calls
-// with the same mask and N.  Teams form per k (lanes whose request k asks for
-// a slice of one class).  A request k that some lane makes for a run of
-// slices, a whole block or segments sends that k through malloc_team for
-// every lane.
-template <int N>
-GAL_DEVICE_INLINE void malloc_n(const state *s, const uint64_t (&size)[N], void *(&out)[N], uint32_t callers) {
-  const int T = (int)s->num_trees;
-  const uint32_t lane = lane_id();
-  const uint32_t lt = lanemask_lt();
-  const uint32_t group = team_group(s);
-  const uint64_t tid = thread_linear_id();
-  uint32_t tree[N];
-  bool need[N], fast[N];
-#pragma unroll
-  for (int k = 0; k < N; k++) {
-    out[k] = nullptr;
-    const int t = (size[k] >> s->min_shift) == 0 ? 0 : ceil_log2(size[k]) - (int)s->min_shift;
-    tree[k] = (uint32_t)t;
-    need[k] = t < T;
-    fast[k] = true;
-    if (__ballot_sync(callers, !need[k])) {  // warp-uniform
-      out[k] = malloc_team(s, size[k], callers);
-      need[k] = fast[k] = false;
-    }
-  }
-  for (int attempt = 0; attempt < SLICE_ATTEMPTS; attempt++) {
-    uint32_t team[N], blk[N], slot[N];
-    int last[N];
-    bool any = false;
-    // the teams and their pinned blocks; every lane of a team reads the same
-    // slot word in the same instruction, and the leader's copy decides
-#pragma unroll
-    for (int k = 0; k < N; k++) {
-      const uint32_t act = __ballot_sync(callers, need[k]);
-      team[k] = __match_any_sync(callers, need[k] ? tree[k] : 0xFFFFFFFFu) & group & act;
-      uint32_t seen = NOBLK;
-      slot[k] = 0;
-      if (need[k]) slot[k] = pick_slot(s, tree[k], seen);
-      const int leader = need[k] ? __ffs(team[k]) - 1 : (int)lane;
-      last[k] = need[k] ? 31 - __clz(team[k]) : (int)lane;
-      blk[k] = __shfl_sync(callers, seen, leader);
-      any |= act != 0;
-    }
-    if (!any) break;
-    // the claims, one atomic per team and k, issued back to back
-    unsigned long long old[N];
-#pragma unroll
-    for (int k = 0; k < N; k++) {
-      old[k] = 0;
-      if (need[k] && blk[k] != NOBLK && (int)lane == last[k])
-        old[k] = atomicAdd(mword_ptr(s, blk[k]), (unsigned long long)__popc(team[k]));
-    }
-    bool refill[N];
-#pragma unroll
-    for (int k = 0; k < N; k++) {
-      refill[k] = false;
-      old[k] = __shfl_sync(callers, old[k], last[k]);
-      const bool mine = need[k] && blk[k] != NOBLK;
-      const uint64_t alloc = (old[k] & 0xFFFFFFFFull) + (uint32_t)__popc(team[k] & lt);
-      const bool valid = mine && alloc <= SLICES_PER_BLOCK - 1;
-      const bool foreign = (uint32_t)(old[k] >> 32) != tree[k];
-      uint32_t rep = __ballot_sync(callers, valid && alloc == SLICES_PER_BLOCK - 1) & team[k];
-      const bool exhausted = mine && !foreign && (__ballot_sync(callers, valid) & team[k]) == 0;
-      if (exhausted && (old[k] & 0xFFFFFFFFull) >= SLICES_PER_BLOCK + STUCK_MARGIN) rep = team[k];
-      if (mine && rep && (int)lane == __ffs(team[k]) - 1) {
-        if (s->use_spares) refill[k] = swap_spare(s, tree[k], slot[k], blk[k], tid);
-        else replace_block(s, tree[k], slot[k], blk[k], tid);
-      }
-      if (valid) {
-        if (!foreign) {
-          out[k] = slice_ptr(s, blk[k], alloc, tree[k]);
-          need[k] = false;
-        } else {
-          credit_frees(s, blk[k], 1);  // Block::check_valid failed: give the slice back
-        }
-      }
-    }
-    __syncwarp(callers);
-#pragma unroll
-    for (int k = 0; k < N; k++)
-      if (refill[k]) refill_spare(s, tree[k], slot[k], tid);
-  }
-#pragma unroll
-  for (int k = 0; k < N; k++)
-    if (fast[k]) out[k] = handed_out(s, out[k], size[k]);
-}
-
 // multi-segment free (gallatin.cuh:1394-1417, 1283-1302), id reset first
 GAL_DEVICE_COLD void free_segment_run(const state *s, uint64_t seg, uint16_t tree) {
   uint32_t count = (uint32_t)tree - s->num_trees - 1;

@@ -386,13 +386,12 @@ def test_cached_block_churn_payloads_and_fresh_trees(G, mode):
         g.close()
 
 
-@pytest.mark.parametrize("mode", [256, 128 | 512, 256 | 512 | (1 << 11), 128 | (1 << 11),
-                                  (2 << 11) | 512, 8 | 256 | 512 | (1 << 11)])
+@pytest.mark.parametrize("mode", [256, 128 | 512, 256 | 512, 8 | 256 | 512])
 def test_per_thread_churn_forms_payloads_and_fresh_trees(G, mode):
-    """The per-thread malloc kernel compiled for 3 or 4 CTAs per SM, lanes
-    serving 1, 2 or 4 requests each through gal::malloc_n, and the free
-    kernel compiled for 4 CTAs per SM: every malloc served, payloads intact,
-    frees balance the mallocs, and after trim the trees are fresh again."""
+    """The per-thread malloc kernel compiled for 3 or 4 CTAs per SM and the
+    free kernel compiled for 4 CTAs per SM, with and without payloads: every
+    malloc served, payloads intact, frees balance the mallocs, and after trim
+    the trees are fresh again."""
     g = G.Gallatin.generate_on_device(32 << 30, 42, spare_blocks=1, pinned_slots_first=0,
                                       bytes_per_segment=64 << 20, gather_unlocked_below=16)
     try:
