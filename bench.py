@@ -670,6 +670,7 @@ def main():
             server[key] = {"ops_per_s": (sr.mallocs_ok + sr.frees) / (sr.ms_total / 1e3),
                            "ms_per_step": sr.ms_total / 3, "violations": int(sr.stamp_mismatch + sr.misaligned),
                            "failed": int(sr.mallocs_failed), "status": int(sr.status),
+                           "error_word": int(sr.error_word),
                            "grid": int(sr.grid), "server_ctas": int(sr.server_ctas), "graph": bool(sr.graph)}
             progress(f"server {key} done")
         server["streams"] = [list(s) for s in SERVER_STREAMS]

@@ -25,7 +25,8 @@
 //   * every spin-wait is bounded by state::spin_limit and reports through the
 //     error word instead of trapping (the reference traps, gallatin.cuh:87);
 //   * a vEB remove re-checks the emptied child word after clearing its
-//     summary bit, closing the race that hides a non-empty word;
+//     summary bit, with acquire-release fences ordering each thread's word
+//     and summary accesses, closing the race that hides a non-empty word;
 //   * a failed contiguous-run search does not roll back bits it never took
 //     (the reference's exit rollback, veb.cuh:447);
 //   * a multi-segment free resets the segment's tree id before returning its
@@ -180,6 +181,10 @@ GAL_DEVICE_INLINE uint16_t ld_rlx(const uint16_t *p) {
   asm volatile("ld.relaxed.gpu.global.u16 %0, [%1];" : "=h"(v) : "l"(p) : "memory");
   return v;
 }
+// acquire-release fence at device scope: orders this thread's earlier and
+// later memory accesses (lighter than __threadfence's sequentially
+// consistent one)
+GAL_DEVICE_INLINE void fence_acq_rel() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 GAL_DEVICE_INLINE uint64_t amo_or(uint64_t *p, uint64_t v) {
   return atomicOr((unsigned long long *)p, (unsigned long long)v);
 }
@@ -261,7 +266,15 @@ GAL_DEVICE_INLINE bool veb_query(const veb_ref &v, uint64_t x) {
   return (ld_rlx(v.word(v.sh->layers - 1, x >> 6)) >> (x & 63)) & 1ULL;
 }
 
-// veb_tree::remove (veb.cuh:737-755) plus the child re-check
+// veb_tree::remove (veb.cuh:737-755) plus the child re-check.  A remove that
+// empties a word clears the word's summary bit, then reads the word again: an
+// insert that refilled it meanwhile set the word's bit before the summary's,
+// and acquire-release fences on both sides order the two accesses of each
+// thread (the insert's set of the summary publishes its set of the word), so
+// either the insert's summary set lands after this clear or this re-read sees
+// the refilled word.  Without them a clear could land after the insert's set
+// while the re-read still saw the empty word, leaving a non-empty word behind
+// a clear summary bit, where top-down searches never find its items.
 GAL_DEVICE_INLINE bool veb_remove(const veb_ref &v, uint64_t x) {
   int layer = (int)v.sh->layers - 1;
   uint64_t high = x >> 6;
@@ -273,7 +286,9 @@ GAL_DEVICE_INLINE bool veb_remove(const veb_ref &v, uint64_t x) {
     layer -= 1;
     low = (int)(high & 63);
     high >>= 6;
+    fence_acq_rel();
     old = amo_and(v.word(layer, high), ~(1ULL << low));
+    fence_acq_rel();
     if (ld_rlx(child) != 0) {  // an insert raced in: keep the summary bit
       amo_or(v.word(layer, high), 1ULL << low);
       break;
@@ -282,7 +297,8 @@ GAL_DEVICE_INLINE bool veb_remove(const veb_ref &v, uint64_t x) {
   return true;
 }
 
-// veb_tree::insert_force_update (veb.cuh:775-798)
+// veb_tree::insert_force_update (veb.cuh:775-798); the fence orders each
+// word's set before its summary's (see veb_remove)
 GAL_DEVICE_INLINE bool veb_insert(const veb_ref &v, uint64_t x) {
   int layer = (int)v.sh->layers - 1;
   uint64_t high = x >> 6;
@@ -293,6 +309,7 @@ GAL_DEVICE_INLINE bool veb_insert(const veb_ref &v, uint64_t x) {
     layer -= 1;
     low = (int)(high & 63);
     high >>= 6;
+    fence_acq_rel();
     old = amo_or(v.word(layer, high), 1ULL << low);
   }
   return true;
@@ -463,6 +480,7 @@ GAL_DEVICE_COLD uint64_t veb_gather_multiple(const veb_ref &v, uint64_t n) {
     for (uint64_t wb = lo; wb < lo + n; wb++) {
       if (ld_rlx(v.word(i + 1, wb)) != 0) continue;
       amo_and(v.word(i, wb / 64), ~(1ULL << (wb % 64)));
+      fence_acq_rel();
       // an insert that refilled the word between the load and the clear found
       // the summary bit still set and left it: put it back, as veb_remove does
       if (ld_rlx(v.word(i + 1, wb)) != 0) amo_or(v.word(i, wb / 64), 1ULL << (wb % 64));
@@ -495,6 +513,7 @@ GAL_DEVICE_COLD void veb_return_multiple(const veb_ref &v, uint64_t start, uint6
     uint64_t hi = (lo + n - 1) / 64 + 1;
     lo = lo / 64;
     n = hi - lo;
+    fence_acq_rel();  // the words below are set before their summaries (see veb_remove)
     for (uint64_t wb = lo; wb < lo + n; wb++)
       if (ld_rlx(v.word(i + 1, wb)) != 0) amo_or(v.word(i, wb / 64), 1ULL << (wb % 64));
   }
