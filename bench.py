@@ -61,7 +61,7 @@ WORKLOAD = ("mixed-size churn: arena 128 GiB as 2,048 segments of 64 MiB (Gallat
             "round, drain; uint32 payload written+checked")
 # the knobs of this library's throughput settings (gal_config); the reference has none of them
 TUNED = dict(pinned_slots_first=0, pinned_slots_min=0, gather_unlocked_below=16,
-             bytes_per_segment=SEGMENT, spare_blocks=1, block_layout=1)
+             bytes_per_segment=SEGMENT, spare_blocks=1, block_layout=1, l2_fetch_bytes=32)
 # gal_bench_churn modes: bit 0 CTA claim, bit 2 cached pinned blocks, bit 3 allocator-only,
 # bits 7 / 8 the plain or cached malloc kernel compiled for 4 / 3 CTAs of 256 threads per SM
 FORMS = {"plain": 0, "cta": 1, "cached": 4}
@@ -97,6 +97,9 @@ def parse():
                    help="plain and cached forms: CTAs of 256 threads per SM the malloc kernel's "
                         "registers must allow (0: the kernel's own count -- no bound for plain, 2 "
                         "for cached)")
+    p.add_argument("--l2-fetch-bytes", type=int, default=32, choices=[0, 32, 64, 128],
+                   help="gal_config.l2_fetch_bytes of the tuned allocators (0: leave the context's "
+                        "setting)")
     p.add_argument("--free-ctas-per-sm", type=int, default=4, choices=[0, 4],
                    help="free kernel: CTAs of 256 threads per SM its registers must allow (0: no bound)")
     p.add_argument("--slots", type=int, default=0,
@@ -208,6 +211,16 @@ def sum_over_ranks(x, world):
     return _reduce_over_ranks(x, world, "SUM")
 
 
+def set_l2_fetch_bytes(nbytes):
+    """Hint the largest L2 fetch for this process's context
+    (cudaLimitMaxL2FetchGranularity); the setting ends with the process."""
+    import ctypes as C
+    cudart = C.CDLL(os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "lib64", "libcudart.so"))
+    rc = cudart.cudaDeviceSetLimit(C.c_int(5), C.c_size_t(nbytes))
+    if rc != 0:
+        raise RuntimeError(f"cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, {nbytes}) returned {rc}")
+
+
 def measured_hbm_peak():
     """HBM copy bandwidth (GB/s) measured on this GPU model (MEASURED_PEAKS.json),
     else the fallback figure of one earlier GB300 measurement."""
@@ -285,6 +298,12 @@ def run_reference(args, world, rank):
         v = ops / (float(ms.sum()) / 1e3)
         ms16, st16 = churn(16, max(3, args.steps // 4))
         v16 = float(st16[0] + st16[3]) / (float(ms16.sum()) / 1e3)
+        # the same 64 MiB churn once more with the context hint this library's
+        # tuned settings give (gal_config.l2_fetch_bytes = 32); last, as the
+        # hint stays for the rest of the process
+        set_l2_fetch_bytes(32)
+        msh, sth = churn(64, max(3, args.steps // 4))
+        vh = float(sth[0] + sth[3]) / (float(msh.sum()) / 1e3)
         line.update({
             "value": v, "ms_per_step": float(ms.mean()), "scaling": "weak", "vs_baseline": None,
             "dtype": "u64", "data": "synthetic (Philox4x32-10 seed 1; sizes log-uniform 16 B-4 KiB rounded to pow2)",
@@ -296,6 +315,11 @@ def run_reference(args, world, rank):
                 "segment_bytes": 16 << 20, "ops_per_s": v16, "ms_per_step": float(ms16.mean()),
                 "mallocs_failed": int(st16[1]), "payload_mismatch": int(st16[2]),
                 "note": "the reference's global type Gallatin<16MiB,16,4096> on the same churn"},
+            "reference_l2_fetch_32": {
+                "segment_bytes": 64 << 20, "ops_per_s": vh, "ms_per_step": float(msh.mean()),
+                "mallocs_failed": int(sth[1]), "payload_mismatch": int(sth[2]),
+                "note": "the same 64 MiB churn after cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, "
+                        "32), the context hint of this library's tuned settings; `value` runs without it"},
             "cpu_baseline": {"value": v, "unit": "ops/s", "cores": 1, "kind": "reference",
                              "sample": "the whole workload, the reference's own CUDA build on the GPU (it has "
                                        "no CPU implementation of this path)"},
@@ -493,6 +517,7 @@ def main():
     import torch
     torch.cuda.set_device(local)
     import gallatin_gb300 as G
+    TUNED["l2_fetch_bytes"] = args.l2_fetch_bytes
 
     N, R = args.threads_per_round, args.rounds
     arena = args.arena_gib << 30
@@ -718,7 +743,8 @@ def main():
                 + "; persistent free phase, four frees per lane, segment classes staged in shared memory, "
                   "one free-counter atomic per warp team; one CUDA graph per step",
         "knobs": dict(TUNED, note="gal_config fields; pinned_slots_first=0 means one pinned slot per SM "
-                                  "in every class"),
+                                  "in every class; l2_fetch_bytes is a hint for the whole CUDA context, "
+                                  "so the allocators the run builds after the headline's see it too"),
         "mallocs_per_step": res.mallocs_ok / args.steps, "mallocs_failed": int(res.mallocs_failed),
         "payload_mismatch": int(res.payload_mismatch), "device_error_word": int(errors | res.error_word),
         "wall_s_timed": wall,

@@ -51,6 +51,7 @@ class GalConfig(C.Structure):
         ("spare_blocks", C.c_uint32),
         ("zero_fill", C.c_uint32),
         ("block_layout", C.c_uint32),
+        ("l2_fetch_bytes", C.c_uint32),
     ]
 
 

@@ -341,12 +341,22 @@ int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot
   if (cfg.team_width > 32 || (cfg.team_width & (cfg.team_width - 1))) return GAL_ERR_ARGS;
   if (cfg.arena_kind > GAL_ARENA_MANAGED) return GAL_ERR_ARGS;
   if (cfg.spare_blocks > 1 || cfg.zero_fill > 1 || cfg.block_layout > 1) return GAL_ERR_ARGS;
+  if (cfg.l2_fetch_bytes != 0 && cfg.l2_fetch_bytes != 32 && cfg.l2_fetch_bytes != 64 &&
+      cfg.l2_fetch_bytes != 128)
+    return GAL_ERR_ARGS;
   const uint32_t T = log2u(cfg.max_size) - log2u(cfg.min_size) + 1;
   const uint64_t S = num_bytes / cfg.bytes_per_segment;
   if (T > GAL_MAX_TREES || S == 0 || S + T + 1 >= 0xFFFF) return GAL_ERR_ARGS;
   const uint32_t bps_shift = log2u(cfg.bytes_per_segment) - log2u(cfg.min_size) - 12;
   const uint64_t nblocks = S << bps_shift;
   if (nblocks >= 0xFFFFFFFFull) return GAL_ERR_ARGS;
+  if (cfg.l2_fetch_bytes) {  // a hint for the current device's whole context
+    cudaError_t e = cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, cfg.l2_fetch_bytes);
+    if (e != cudaSuccess) {
+      fprintf(stderr, "gallatin_gb300: setting the L2 fetch granularity failed: %s\n", cudaGetErrorString(e));
+      return GAL_ERR_CUDA;
+    }
+  }
 
   gal_handle *h = new gal_handle();
   h->cfg = cfg;
@@ -548,6 +558,7 @@ int gal_config_default(gal_config *cfg) {
   cfg->spare_blocks = 0;
   cfg->zero_fill = 0;
   cfg->block_layout = GAL_BLOCK_LAYOUT_RECORD;
+  cfg->l2_fetch_bytes = 0;
   return GAL_OK;
 }
 

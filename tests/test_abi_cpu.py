@@ -90,6 +90,8 @@ def test_ctypes_mirrors_have_the_header_layout(tmp_path, ctype, mirror):
     dict(arena_kind=3),                        # device, host or managed only
     dict(spare_blocks=2),                      # off or on
     dict(zero_fill=2),                         # off or on
+    dict(block_layout=2),                      # dense or record
+    dict(l2_fetch_bytes=48),                   # 0, 32, 64 or 128
 ])
 def test_invalid_config_rejected_before_device_use(L, kw):
     import gallatin_gb300 as G
