@@ -686,7 +686,7 @@ def main():
     server = {}
     if world == 1:
         for key, direct in (("server", False), ("direct", True)):
-            gs = G.Gallatin.generate_on_device(32 << 30, ALLOC_SEED, **TUNED)
+            gs = G.Gallatin.generate_on_device(64 << 30, ALLOC_SEED, **TUNED)
             try:
                 sms, sr = gs.bench_server(SERVER_STREAMS, server_pct=25, direct=direct, use_graph=True,
                                           warmup=1, steps=3)

@@ -27,7 +27,11 @@
 namespace gal {
 
 static constexpr uint32_t SERVER_ERR_TIMEOUT = 0x1u;
-static constexpr int SERVER_RUNS = 8;  // runs a server batch may use per class
+// positions a server warp takes at once (its lanes answer them 32 at a time):
+// with many server warps a take of one warp's width left most takes a few
+// requests each, and the warps spent their time contending on the classes'
+// `taken` counters instead of answering
+static constexpr uint32_t SERVER_BATCH = 256;
 
 struct server_rings {
   unsigned long long *entries;   // [num_trees << cap_shift]
@@ -120,9 +124,9 @@ struct server_smem {
 
 // The server loop (every thread of a server CTA calls it).  Each warp serves
 // on its own, without CTA barriers: it sweeps the classes, starting at a
-// class of its own, takes a batch of up to 32 reserved positions of a class,
-// claims their slices with one atomicAdd per run (lane 0), and every lane
-// answers one request.  Returns once no producer is left and every reserved
+// class of its own, takes a batch of up to SERVER_BATCH reserved positions of
+// a class, claims their slices with one atomicAdd per run (lane 0), and the
+// lanes answer the requests 32 at a time.  Returns once no producer is left and every reserved
 // position is served, or at the deadline.
 GAL_DEVICE_INLINE void server_loop(const state *s, const server_rings &r, server_smem &sm, uint64_t t0) {
   const uint32_t T = s->num_trees;
@@ -142,9 +146,9 @@ GAL_DEVICE_INLINE void server_loop(const state *s, const server_rings &r, server
       uint32_t m = 0, nruns = 0, spare_slot[2] = {NOBLK, NOBLK};
       uint32_t rb[2] = {NOBLK, NOBLK}, rs[2] = {0, 0}, rl[2] = {0, 0};
       if (lane == 0) {
-        m = server_take(r, t, 32, &first);
+        m = server_take(r, t, SERVER_BATCH, &first);
         uint32_t need = m;
-        while (need && nruns < 2) {  // 32 slices: at most one crossing of a block's end
+        while (need && nruns < 2) {  // at most SERVER_BATCH slices: one crossing of a block's end
           uint32_t blk, start, ss;
           const uint32_t got = claim_run(s, t, need, rc, blk, start, ss);
           spare_slot[nruns] = ss;
@@ -163,32 +167,34 @@ GAL_DEVICE_INLINE void server_loop(const state *s, const server_rings &r, server
       const uint32_t b0 = __shfl_sync(0xFFFFFFFFu, rb[0], 0), b1 = __shfl_sync(0xFFFFFFFFu, rb[1], 0);
       const uint32_t s0 = __shfl_sync(0xFFFFFFFFu, rs[0], 0), s1 = __shfl_sync(0xFFFFFFFFu, rs[1], 0);
       const uint32_t l0 = __shfl_sync(0xFFFFFFFFu, rl[0], 0), l1 = __shfl_sync(0xFFFFFFFFu, rl[1], 0);
-      if (lane < m) {
-        const uint64_t pos = first + lane;
-        unsigned long long *e = r.entries + ((uint64_t)t << r.cap_shift) + (pos & ((1ull << r.cap_shift) - 1));
-        const unsigned long long lap = (pos >> r.cap_shift) & 0xFFFFFFull;
-        unsigned long long v;
-        bool ok = true;
-        for (uint32_t i = 0; ((v = ld_acquire(e)) >> 40) != lap || v == 0ull; i++) {  // not yet published
-          if (global_ns() - t0 > r.deadline_ns) {
-            atomicOr(r.status, SERVER_ERR_TIMEOUT);
-            ok = false;
-            break;
+      for (uint32_t j = lane; j < ((m + 31u) & ~31u); j += 32u) {  // whole warps each pass
+        if (j < m) {
+          const uint64_t pos = first + j;
+          unsigned long long *e = r.entries + ((uint64_t)t << r.cap_shift) + (pos & ((1ull << r.cap_shift) - 1));
+          const unsigned long long lap = (pos >> r.cap_shift) & 0xFFFFFFull;
+          unsigned long long v;
+          bool ok = true;
+          for (uint32_t i = 0; ((v = ld_acquire(e)) >> 40) != lap || v == 0ull; i++) {  // not yet published
+            if (global_ns() - t0 > r.deadline_ns) {
+              atomicOr(r.status, SERVER_ERR_TIMEOUT);
+              ok = false;
+              break;
+            }
+            __nanosleep(i < 4 ? 32 : 256);
           }
-          __nanosleep(i < 4 ? 32 : 256);
+          if (ok) {
+            void *p = nullptr;
+            if (j < l0) p = slice_ptr(s, b0, s0 + j, t);
+            else if (j < l0 + l1) p = slice_ptr(s, b1, s1 + j - l0, t);
+            else p = malloc_slices<false>(s, t, 1, active_lanes());  // the runs fell short
+            if (p && s->zero_fill) zero_fill(p, 1ull << (s->min_shift + t));  // the whole slice
+            const uint64_t slot = (v & ((1ull << 40) - 1)) - 1;
+            st_release(e, 0ull);  // the entry is free for the next lap
+            st_release(r.reply + slot, p ? (unsigned long long)p : 1ull);
+          }
         }
-        if (ok) {
-          void *p = nullptr;
-          if (lane < l0) p = slice_ptr(s, b0, s0 + lane, t);
-          else if (lane < l0 + l1) p = slice_ptr(s, b1, s1 + lane - l0, t);
-          else p = malloc_slices<false>(s, t, 1, active_lanes());  // the runs fell short
-          if (p && s->zero_fill) zero_fill(p, 1ull << (s->min_shift + t));  // the whole slice
-          const uint64_t slot = (v & ((1ull << 40) - 1)) - 1;
-          st_release(e, 0ull);  // the entry is free for the next lap
-          st_release(r.reply + slot, p ? (unsigned long long)p : 1ull);
-        }
+        __syncwarp();
       }
-      __syncwarp();
       if (lane == 0)  // spare blocks of the runs that crossed a block's end, after the replies
         for (int q = 0; q < 2; q++)
           if (spare_slot[q] != NOBLK) refill_spare(s, t, spare_slot[q], thread_linear_id());

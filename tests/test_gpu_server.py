@@ -57,15 +57,15 @@ def test_server_refuses_streams_beyond_runs_of_slices(G):
 
 
 def test_direct_producers_repeated_never_starve(G):
-    """The direct producers, several fresh allocators in a row at the bench's
-    size: segments freed by one class's returns are found again by another
-    class's gathers every time.  (Before the vEB summary updates were fenced,
-    a remove's clear of a summary bit could land after a racing insert's set,
-    hiding a word of free segments from the gathers: one run in three to
-    eight then starved and failed requests.)"""
+    """The direct producers at the bench's size, several fresh 64 GiB
+    allocators in a row: every request is served every time.  (At 32 GiB
+    one run in three to eight ran out of segments: with one pinned slot per
+    SM and a spare each, the pinned blocks of the 2 and 4 KiB classes alone
+    can hold hundreds of 64 MiB segments, and segments gathered ahead when a
+    class takes a segment's last block stay with the class until used.)"""
     streams = [(6_000_000, 16, 128, 0, 1), (4_000_000, 16, 4096, 1, 2), (1_000_000, 1024, 32768, 1, 4)]
     for rep in range(6):
-        g = G.Gallatin.generate_on_device(32 << 30, 42, spare_blocks=1, pinned_slots_first=0,
+        g = G.Gallatin.generate_on_device(64 << 30, 42, spare_blocks=1, pinned_slots_first=0,
                                           bytes_per_segment=64 << 20, gather_unlocked_below=16)
         try:
             ms, r = g.bench_server(streams, server_pct=25, direct=True, use_graph=True, warmup=1, steps=3)
