@@ -61,7 +61,7 @@ WORKLOAD = ("mixed-size churn: arena 128 GiB as 2,048 segments of 64 MiB (Gallat
             "round, drain; uint32 payload written+checked")
 # the knobs of this library's throughput settings (gal_config); the reference has none of them
 TUNED = dict(pinned_slots_first=0, pinned_slots_min=0, gather_unlocked_below=16,
-             bytes_per_segment=SEGMENT, spare_blocks=1, block_layout=1, l2_fetch_bytes=32)
+             bytes_per_segment=SEGMENT, spare_blocks=1, block_layout=1, l2_fetch_bytes=32, gather_ahead=1)
 # gal_bench_churn modes: bit 0 CTA claim, bit 2 cached pinned blocks, bit 3 allocator-only,
 # bits 7 / 8 the plain or cached malloc kernel compiled for 4 / 3 CTAs of 256 threads per SM
 FORMS = {"plain": 0, "cta": 1, "cached": 4}
@@ -100,6 +100,8 @@ def parse():
     p.add_argument("--l2-fetch-bytes", type=int, default=32, choices=[0, 32, 64, 128],
                    help="gal_config.l2_fetch_bytes of the tuned allocators (0: leave the context's "
                         "setting)")
+    p.add_argument("--gather-ahead", type=int, default=1, choices=[0, 1],
+                   help="gal_config.gather_ahead of the tuned allocators")
     p.add_argument("--free-ctas-per-sm", type=int, default=4, choices=[0, 4],
                    help="free kernel: CTAs of 256 threads per SM its registers must allow (0: no bound)")
     p.add_argument("--slots", type=int, default=0,
@@ -518,6 +520,7 @@ def main():
     torch.cuda.set_device(local)
     import gallatin_gb300 as G
     TUNED["l2_fetch_bytes"] = args.l2_fetch_bytes
+    TUNED["gather_ahead"] = args.gather_ahead
 
     N, R = args.threads_per_round, args.rounds
     arena = args.arena_gib << 30
@@ -688,7 +691,7 @@ def main():
         for key, direct in (("server", False), ("direct", True)):
             gs = G.Gallatin.generate_on_device(64 << 30, ALLOC_SEED, **TUNED)
             try:
-                sms, sr = gs.bench_server(SERVER_STREAMS, server_pct=25, direct=direct, use_graph=True,
+                sms, sr = gs.bench_server(SERVER_STREAMS, server_pct=10, direct=direct, use_graph=True,
                                           warmup=1, steps=3)
             finally:
                 gs.close()

@@ -52,6 +52,7 @@ class GalConfig(C.Structure):
         ("zero_fill", C.c_uint32),
         ("block_layout", C.c_uint32),
         ("l2_fetch_bytes", C.c_uint32),
+        ("gather_ahead", C.c_uint32),
     ]
 
 

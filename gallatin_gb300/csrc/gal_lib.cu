@@ -344,6 +344,7 @@ int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot
   if (cfg.l2_fetch_bytes != 0 && cfg.l2_fetch_bytes != 32 && cfg.l2_fetch_bytes != 64 &&
       cfg.l2_fetch_bytes != 128)
     return GAL_ERR_ARGS;
+  if (cfg.gather_ahead > 1) return GAL_ERR_ARGS;
   const uint32_t T = log2u(cfg.max_size) - log2u(cfg.min_size) + 1;
   const uint64_t S = num_bytes / cfg.bytes_per_segment;
   if (T > GAL_MAX_TREES || S == 0 || S + T + 1 >= 0xFFFF) return GAL_ERR_ARGS;
@@ -374,6 +375,7 @@ int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot
   st.smid_override = cfg.smid_override;
   st.spin_limit = cfg.spin_limit ? cfg.spin_limit : (1u << 16);
   st.gather_unlocked_below = cfg.gather_unlocked_below;
+  st.gather_ahead = cfg.gather_ahead;
   st.team_width = cfg.team_width ? cfg.team_width : 32;
   st.use_spares = cfg.spare_blocks ? 1u : 0u;
   st.zero_fill = cfg.zero_fill;
@@ -559,6 +561,7 @@ int gal_config_default(gal_config *cfg) {
   cfg->zero_fill = 0;
   cfg->block_layout = GAL_BLOCK_LAYOUT_RECORD;
   cfg->l2_fetch_bytes = 0;
+  cfg->gather_ahead = 1;
   return GAL_OK;
 }
 

@@ -116,6 +116,16 @@ typedef struct gal_config {
                                    32 B instead of a whole line: the mixed
                                    churn's free phase read 2.8x fewer DRAM
                                    bytes at 32.                                 */
+  uint32_t gather_ahead;        /* 1 (default): a request that takes the last
+                                   block of a class's segment also gathers the
+                                   class's next segment, as the reference does
+                                   (gallatin.cuh:1598-1612).  0: segments are
+                                   gathered only by requests that find their
+                                   class without one.  Segments gathered ahead
+                                   stay with their class until used; with one
+                                   pinned slot per SM and spares, classes that
+                                   turn over many blocks hold many of them.
+                                   0 changes serial results.                  */
 } gal_config;
 
 /* Block counter layouts (gal_config.block_layout). */

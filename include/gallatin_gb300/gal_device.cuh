@@ -83,6 +83,7 @@ struct state {
   uint32_t spin_limit;
   uint32_t total_slots;
   uint32_t gather_unlocked_below;  // see gal_config
+  uint32_t gather_ahead;           // see gal_config
   uint32_t team_width;             // see gal_config (1..32, a power of two)
   uint32_t use_spares;             // see gal_config.spare_blocks
   uint32_t zero_fill;              // see gal_config.zero_fill
@@ -689,7 +690,7 @@ GAL_DEVICE_COLD uint32_t request_block(const state *s, uint32_t tree, uint64_t t
     uint32_t blk = get_block(s, seg, tree, last);
     if (last) {
       veb_remove(sub, seg);
-      if (unlocked || try_lock(s, tree)) {
+      if (s->gather_ahead && (unlocked || try_lock(s, tree))) {
         gather_new_segment(s, tree);
         if (!unlocked) unlock(s, tree);
       }
