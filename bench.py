@@ -695,7 +695,7 @@ def main():
                                           warmup=1, steps=3)
             finally:
                 gs.close()
-            server[key] = {"ops_per_s": (sr.mallocs_ok + sr.frees) / (sr.ms_total / 1e3),
+            server[key] = {"ops_per_s": (sr.mallocs_ok + sr.frees) / (sr.ms_total / 1e3) if sr.ms_total else None,
                            "ms_per_step": sr.ms_total / 3, "violations": int(sr.stamp_mismatch + sr.misaligned),
                            "failed": int(sr.mallocs_failed), "status": int(sr.status),
                            "error_word": int(sr.error_word),

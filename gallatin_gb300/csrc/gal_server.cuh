@@ -14,12 +14,18 @@
 //
 // Rings: class t has 2^cap_shift entries; position p of class t lives in
 // entry p mod 2^cap_shift and holds (lap << 40) | (reply slot + 1), lap =
-// p >> cap_shift (mod 2^24), 0 when empty.  A producer reserves positions
+// p >> cap_shift (mod 2^24), while a request waits in it, and lap << 40 (slot
+// bits zero) while it is free for that lap.  A producer reserves positions
 // with atomicAdd on the class's tail (one per warp team), waits for its entry
-// to be empty (the server of the previous lap clears it) and publishes the
-// request; a server takes positions with a CAS on the class's `taken`
-// counter, waits for each entry to carry its own lap, answers in the reply
-// slot (the pointer, or 1 for no memory) and clears the entry.
+// to be free for its own lap (the server of the previous lap hands it on) and
+// publishes the request; a server takes positions with a CAS on the class's
+// `taken` counter, waits for each entry to carry its own lap's request,
+// answers in the reply slot (the pointer, or 1 for no memory) and hands the
+// entry to the next lap.  Naming the lap in the free state matters once the
+// ring wraps: with a bare "empty", a request of the next lap could take an
+// entry whose own lap was still waiting to publish, and a server warp holding
+// that position while it answers a batch in order could wait on the server
+// warp that needs the later request answered first.
 #pragma once
 
 #include "gal_batch.cuh"
@@ -57,8 +63,15 @@ GAL_DEVICE_INLINE unsigned long long ld_acquire(const unsigned long long *p) {
 GAL_DEVICE_INLINE void st_release(unsigned long long *p, unsigned long long v) {
   asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
+GAL_DEVICE_INLINE unsigned long long ring_lap(uint64_t pos, uint32_t cap_shift) {
+  return (unsigned long long)((pos >> cap_shift) & 0xFFFFFFull);
+}
 GAL_DEVICE_INLINE unsigned long long ring_entry(uint64_t pos, uint32_t cap_shift, uint64_t slot) {
-  return ((unsigned long long)((pos >> cap_shift) & 0xFFFFFFull) << 40) | (slot + 1);
+  return (ring_lap(pos, cap_shift) << 40) | (slot + 1);
+}
+// the entry free for the lap of `pos` (all zero for lap 0, the state at set-up)
+GAL_DEVICE_INLINE unsigned long long ring_free(uint64_t pos, uint32_t cap_shift) {
+  return ring_lap(pos, cap_shift) << 40;
 }
 
 // A producer lane's request for `size` bytes, answered by a server CTA of the
@@ -79,7 +92,8 @@ GAL_DEVICE_INLINE void *server_malloc(const state *s, const server_rings &r, uin
   base = __shfl_sync(callers, base, leader);
   const uint64_t pos = base + (uint64_t)__popc(team & lanemask_lt());
   unsigned long long *e = r.entries + ((uint64_t)t << r.cap_shift) + (pos & ((1ull << r.cap_shift) - 1));
-  for (uint32_t i = 0; ld_acquire(e) != 0ull; i++) {  // the previous lap's request still unserved
+  const unsigned long long mine = ring_free(pos, r.cap_shift);
+  for (uint32_t i = 0; ld_acquire(e) != mine; i++) {  // the previous lap's request still unserved
     if (global_ns() - t0 > r.deadline_ns) {
       atomicOr(r.status, SERVER_ERR_TIMEOUT);
       return nullptr;
@@ -171,10 +185,11 @@ GAL_DEVICE_INLINE void server_loop(const state *s, const server_rings &r, server
         if (j < m) {
           const uint64_t pos = first + j;
           unsigned long long *e = r.entries + ((uint64_t)t << r.cap_shift) + (pos & ((1ull << r.cap_shift) - 1));
-          const unsigned long long lap = (pos >> r.cap_shift) & 0xFFFFFFull;
+          const unsigned long long lap = ring_lap(pos, r.cap_shift);
           unsigned long long v;
           bool ok = true;
-          for (uint32_t i = 0; ((v = ld_acquire(e)) >> 40) != lap || v == 0ull; i++) {  // not yet published
+          for (uint32_t i = 0; ((v = ld_acquire(e)) >> 40) != lap || (v & ((1ull << 40) - 1)) == 0ull;
+               i++) {  // not yet published
             if (global_ns() - t0 > r.deadline_ns) {
               atomicOr(r.status, SERVER_ERR_TIMEOUT);
               ok = false;
@@ -189,7 +204,7 @@ GAL_DEVICE_INLINE void server_loop(const state *s, const server_rings &r, server
             else p = malloc_slices<false>(s, t, 1, active_lanes());  // the runs fell short
             if (p && s->zero_fill) zero_fill(p, 1ull << (s->min_shift + t));  // the whole slice
             const uint64_t slot = (v & ((1ull << 40) - 1)) - 1;
-            st_release(e, 0ull);  // the entry is free for the next lap
+            st_release(e, ring_free(pos + (1ull << r.cap_shift), r.cap_shift));  // free for the next lap
             st_release(r.reply + slot, p ? (unsigned long long)p : 1ull);
           }
         }
