@@ -9,11 +9,17 @@ ranks them by malloc+free ops/s:
   max_size           {4096, 16384} B
   pinned slots       {one per SM, 128 halving to 4}   (block-buffer breadth)
   gather_unlocked_below {0, 16}            (classes that gather without a lock)
-  malloc form        {per-thread teams, one CTA claim per class, persistent
-                      CTAs with the pinned blocks cached in shared memory}
-                                           (aggregation width of the claims)
+  malloc form        {per-thread teams (registers for 3 CTAs of 256 per SM),
+                      one CTA claim per class, persistent CTAs with the
+                      pinned blocks cached in shared memory (4 per SM)}
+                                           (aggregation width of the claims;
+                                            frees in warp teams from a kernel
+                                            with registers for 4 CTAs per SM)
   spare blocks       {off, on}             (block-buffer depth: a prepared next
                                             block per pinned slot)
+  l2_fetch_bytes     {128, 32}             (the context's L2 fetch hint, set
+                                            by every point, as it outlives
+                                            the allocator)
 
 Combinations the reference rejects (bytes_per_segment < max_size * 4096,
 gallatin.cuh:300) are skipped, so 4 MiB segments drop out for max 4096.
@@ -30,23 +36,25 @@ ARENA = 128 << 30
 
 
 def grid():
-    for seg, mn, mx, slots, unlocked, form, spares in itertools.product(
-            (16, 64), (16, 128), (4096, 16384), (0, 128), (0, 16), ("plain", "cta", "cached"), (0, 1)):
+    for seg, mn, mx, slots, unlocked, form, spares, l2 in itertools.product(
+            (16, 64), (16, 128), (4096, 16384), (0, 128), (0, 16), ("plain", "cta", "cached"), (0, 1),
+            (128, 32)):
         if (seg << 20) < mx * 4096:
             continue
         yield dict(segment_mib=seg, min_size=mn, max_size=mx, slots=slots, unlocked=unlocked,
-                   form=form, spares=spares)
+                   form=form, spares=spares, l2_fetch_bytes=l2)
 
 
 # gal_bench_churn modes of the malloc forms (frees: warp teams, classes staged)
-FORM_MODES = {"plain": 0, "cta": 1, "cached": 4}
+FORM_MODES = {"plain": 256 | 512, "cta": 1 | 512, "cached": 4 | 128 | 512}
 
 
 def run_one(G, knobs, n, rounds, steps, seed=1):
     cfg = dict(bytes_per_segment=knobs["segment_mib"] << 20, min_size=knobs["min_size"],
                max_size=knobs["max_size"], pinned_slots_first=knobs["slots"],
                pinned_slots_min=knobs["slots"] if knobs["slots"] else 0,
-               gather_unlocked_below=knobs["unlocked"], spare_blocks=knobs.get("spares", 0))
+               gather_unlocked_below=knobs["unlocked"], spare_blocks=knobs.get("spares", 0),
+               l2_fetch_bytes=knobs.get("l2_fetch_bytes", 0))
     if knobs["slots"] == 128:
         cfg["pinned_slots_min"] = 4
     g = G.Gallatin.generate_on_device(ARENA, 42, **cfg)
