@@ -101,7 +101,7 @@ def vector_checksum(job_id, n):
     return int((x >> np.uint64(32)).sum(dtype=np.uint64))
 
 
-def schedule(jobs, slots, budget, launch, clock, realtime=True):
+def schedule(jobs, slots, budget, launch, clock, realtime=True, limit_s=None):
     """The admission loop.  jobs: dicts with kind, n, arrival and row.  A job is
     admitted in arrival order once it has arrived (realtime) or at once, as
     soon as a slot is free and the estimated footprints of the running jobs
@@ -109,7 +109,8 @@ def schedule(jobs, slots, budget, launch, clock, realtime=True):
     alone.  launch(job, slot) starts it and returns an object whose query()
     says whether it has finished; clock() gives seconds since the start.
     Returns the admission and completion times per row and the most jobs that
-    ran at once."""
+    ran at once.  With limit_s, a loop still waiting after that many seconds
+    raises TimeoutError instead of polling on."""
     nj = len(jobs)
     pending = deque(sorted(jobs, key=lambda j: j["arrival"]))
     free_slots = list(range(slots))
@@ -119,6 +120,9 @@ def schedule(jobs, slots, budget, launch, clock, realtime=True):
     max_running = 0
     while pending or running:
         now = clock()
+        if limit_s is not None and now > limit_s:
+            raise TimeoutError(f"served loop: {len(pending)} jobs pending and {len(running)} running "
+                               f"after {now:.0f} s")
         for slot, (job, ev) in list(running.items()):
             if ev.query():
                 done_t[job["row"]] = clock()
@@ -175,7 +179,7 @@ class Server:
 
         t0 = time.perf_counter()
         admit_t, done_t, max_running = schedule(jobs, self.slots, self.budget, launch,
-                                                lambda: time.perf_counter() - t0, realtime)
+                                                lambda: time.perf_counter() - t0, realtime, limit_s=300.0)
         wall = time.perf_counter() - t0
         torch.cuda.synchronize()
         res = results.cpu().numpy()

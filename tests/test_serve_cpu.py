@@ -116,3 +116,18 @@ def test_job_grids_and_footprints():
     assert job_ctas(JOB_VECTOR, 1 << 30) == 8 and job_ctas(JOB_QUEUE, 1 << 20) == 4
     assert footprint(JOB_VECTOR, 1 << 24) >= 16 * 4 << 20       # 64 MiB of values at least
     assert footprint(JOB_VECTOR, 1 << 24) <= 4 * 3 * (4 << 20) * 8
+
+
+def test_admission_loop_gives_up_after_its_limit():
+    """A job that never finishes ends the loop with TimeoutError once the
+    clock passes the limit, instead of polling forever."""
+    import pytest
+
+    class Never:
+        def query(self):
+            return False
+
+    ticks = iter(range(10 ** 6))
+    jobs = [{"kind": 0, "n": 1, "arrival": 0.0, "row": 0}]
+    with pytest.raises(TimeoutError):
+        schedule(jobs, 1, 1 << 30, lambda job, slot: Never(), lambda: float(next(ticks)), limit_s=50.0)
