@@ -100,7 +100,7 @@ def parse():
     p.add_argument("--l2-fetch-bytes", type=int, default=32, choices=[0, 32, 64, 128],
                    help="gal_config.l2_fetch_bytes of the tuned allocators (0: leave the context's "
                         "setting)")
-    p.add_argument("--gather-ahead", type=int, default=1, choices=[0, 1, 2],
+    p.add_argument("--gather-ahead", type=int, default=1, choices=[0, 1],
                    help="gal_config.gather_ahead of the tuned allocators")
     p.add_argument("--free-ctas-per-sm", type=int, default=4, choices=[0, 4],
                    help="free kernel: CTAs of 256 threads per SM its registers must allow (0: no bound)")

@@ -344,7 +344,7 @@ int build(uint64_t num_bytes, uint64_t seed, const gal_config *cfg_in, bool boot
   if (cfg.l2_fetch_bytes != 0 && cfg.l2_fetch_bytes != 32 && cfg.l2_fetch_bytes != 64 &&
       cfg.l2_fetch_bytes != 128)
     return GAL_ERR_ARGS;
-  if (cfg.gather_ahead > 2) return GAL_ERR_ARGS;
+  if (cfg.gather_ahead > 1) return GAL_ERR_ARGS;
   const uint32_t T = log2u(cfg.max_size) - log2u(cfg.min_size) + 1;
   const uint64_t S = num_bytes / cfg.bytes_per_segment;
   if (T > GAL_MAX_TREES || S == 0 || S + T + 1 >= 0xFFFF) return GAL_ERR_ARGS;

@@ -119,15 +119,11 @@ typedef struct gal_config {
   uint32_t gather_ahead;        /* 1 (default): a request that takes the last
                                    block of a class's segment also gathers the
                                    class's next segment, as the reference does
-                                   (gallatin.cuh:1598-1612).  2: only when no
-                                   other segment of the class is listed then.
-                                   0: segments are gathered only by requests
-                                   that find their class without one.
-                                   Segments gathered ahead stay with their
-                                   class until used; with one pinned slot per
-                                   SM and spares, classes that turn over many
-                                   blocks hold many of them.  0 and 2 change
-                                   serial results.                            */
+                                   (gallatin.cuh:1598-1612).  0: segments are
+                                   gathered only by requests that find their
+                                   class without one (slower on the mixed
+                                   churn: those requests wait for the
+                                   gather).  0 changes serial results.        */
 } gal_config;
 
 /* Block counter layouts (gal_config.block_layout). */

@@ -690,9 +690,7 @@ GAL_DEVICE_COLD uint32_t request_block(const state *s, uint32_t tree, uint64_t t
     uint32_t blk = get_block(s, seg, tree, last);
     if (last) {
       veb_remove(sub, seg);
-      // gather_ahead 2: only when no other segment of the class is listed
-      const bool ahead = s->gather_ahead == 1 || (s->gather_ahead == 2 && veb_find_first(sub) == FAIL);
-      if (ahead && (unlocked || try_lock(s, tree))) {
+      if (s->gather_ahead && (unlocked || try_lock(s, tree))) {
         gather_new_segment(s, tree);
         if (!unlocked) unlock(s, tree);
       }

@@ -92,7 +92,7 @@ def test_ctypes_mirrors_have_the_header_layout(tmp_path, ctype, mirror):
     dict(zero_fill=2),                         # off or on
     dict(block_layout=2),                      # dense or record
     dict(l2_fetch_bytes=48),                   # 0, 32, 64 or 128
-    dict(gather_ahead=3),                      # off, on, or when the class has no other segment
+    dict(gather_ahead=2),                      # off or on
 ])
 def test_invalid_config_rejected_before_device_use(L, kw):
     import gallatin_gb300 as G
