@@ -446,3 +446,23 @@ def test_exhausted_block_left_in_a_slot_is_replaced(G, torch, spares):
         assert g.error_word() == 0, g.error_info()
     finally:
         g.close()
+
+
+@pytest.mark.parametrize("knobs", [dict(l2_fetch_bytes=32), dict(gather_ahead=0), dict(l2_fetch_bytes=64, gather_ahead=0)])
+def test_context_hint_and_on_demand_gathers_serve_the_churn(G, knobs):
+    """The L2 fetch hint set at create time and segments gathered only on
+    demand leave the results alone: every malloc served, payloads intact,
+    counts balanced, fresh trees after trim."""
+    g = G.Gallatin.generate_on_device(32 << 30, 42, spare_blocks=1, pinned_slots_first=0,
+                                      bytes_per_segment=64 << 20, gather_unlocked_below=16, **knobs)
+    try:
+        fresh = g.export()
+        N, R = 1 << 19, 6
+        ms, r = g.bench_churn(N, R, 1, 256 | 512, True, 1, 2)
+        assert r.mallocs_ok == 2 * N * R and r.mallocs_failed == 0
+        assert r.payload_mismatch == 0 and r.frees == r.mallocs_ok and r.error_word == 0
+        g.trim()
+        assert g.error_word() == 0, g.error_info()
+        assert g.export().diff(fresh, fields=TREE_FIELDS) == []
+    finally:
+        g.close()
