@@ -814,6 +814,8 @@ int gal_replay_warp_trace(gal_handle *h, const uint64_t *steps, uint64_t nsteps,
 int gal_malloc_per_thread(gal_handle *h, const uint64_t *sizes, uint64_t n, void **out, void *stream) {
   if (!h || (n && (!sizes || !out))) return GAL_ERR_ARGS;
   if (!n) return GAL_OK;
+  gal_device_guard on_dev(h->device);  // the handle's device, whatever the caller's current one
+  CUDA_TRY(on_dev.err);
   k_malloc_per_thread<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(h->d_state, sizes, n, out);
   CUDA_TRY(cudaGetLastError());
   return GAL_OK;
@@ -822,6 +824,8 @@ int gal_malloc_per_thread(gal_handle *h, const uint64_t *sizes, uint64_t n, void
 int gal_free_per_thread(gal_handle *h, void *const *ptrs, uint64_t n, void *stream) {
   if (!h || (n && !ptrs)) return GAL_ERR_ARGS;
   if (!n) return GAL_OK;
+  gal_device_guard on_dev(h->device);
+  CUDA_TRY(on_dev.err);
   k_free_per_thread<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(h->d_state, ptrs, n);
   CUDA_TRY(cudaGetLastError());
   return GAL_OK;
@@ -829,6 +833,8 @@ int gal_free_per_thread(gal_handle *h, void *const *ptrs, uint64_t n, void *stre
 
 int gal_trim(gal_handle *h, void *stream) {
   if (!h) return GAL_ERR_ARGS;
+  gal_device_guard on_dev(h->device);
+  CUDA_TRY(on_dev.err);
   k_trim<<<1, 1, 0, (cudaStream_t)stream>>>(h->d_state);
   CUDA_TRY(cudaGetLastError());
   return GAL_OK;
@@ -837,6 +843,8 @@ int gal_trim(gal_handle *h, void *stream) {
 int gal_malloc_batched(gal_handle *h, const uint64_t *sizes, uint64_t n, void **out, void *stream) {
   if (!h || (n && (!sizes || !out))) return GAL_ERR_ARGS;
   if (!n) return GAL_OK;
+  gal_device_guard on_dev(h->device);
+  CUDA_TRY(on_dev.err);
   k_malloc_batched<<<grid_for(n, MALLOC_THREADS), MALLOC_THREADS, 0, (cudaStream_t)stream>>>(h->d_state, sizes,
                                                                                           n, out);
   CUDA_TRY(cudaGetLastError());
@@ -851,6 +859,8 @@ int gal_free_batched_n(gal_handle *h, void *const *ptrs, const unsigned long lon
                        uint64_t max_n, void *stream) {
   if (!h || (max_n && !ptrs)) return GAL_ERR_ARGS;
   if (!max_n) return GAL_OK;
+  gal_device_guard on_dev(h->device);
+  CUDA_TRY(on_dev.err);
   unsigned g = grid_for((max_n + FREE_PER_THREAD - 1) / FREE_PER_THREAD, BATCH_THREADS);
   const size_t stage = h->st.num_segments * 2 <= gal::CLASS_STAGE_BYTES ? h->st.num_segments * 2 : 0;
   if (!h->grid_free) h->grid_free = persistent_grid(h->device, k_free_batched, BATCH_THREADS, stage);

@@ -196,7 +196,11 @@ int gal_config_default(gal_config *cfg);
 /* Build an allocator over `num_bytes` of device memory on the current device.
  * Replaces Gallatin<>::generate_on_device (gallatin.cuh:324-421).  The pinned
  * slots are booted deterministically in the order of the reference's
- * boot_shared_block_container_one_thread (gallatin.cuh:196-221). */
+ * boot_shared_block_container_one_thread (gallatin.cuh:196-221).  The calls
+ * that launch work for a handle (batched and per-thread malloc/free, trim,
+ * the exports) run it on the handle's device, whichever device is current,
+ * and leave the caller's current device as it was; the stream passed must
+ * belong to that device. */
 int gal_create(uint64_t num_bytes, uint64_t seed, const gal_config *cfg, gal_handle **out);
 
 /* Same as gal_create without the boot (pinned slots empty); for state import. */
