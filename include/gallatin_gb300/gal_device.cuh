@@ -881,6 +881,19 @@ GAL_DEVICE_INLINE void slot_cache_init(slot_cache &c) {
   }
 }
 
+// The rare part of a claim, out of line so the claim's common path keeps few
+// values live across calls: credits the slices this lane gives back and, for
+// the team's leader when the block must be replaced, swaps in the slot's spare
+// (or replaces the block).  Returns whether the spare wants a refill.
+GAL_DEVICE_COLD bool claim_slow_path(const state *s, uint32_t tree, uint32_t slot, uint32_t blk, uint32_t credit,
+                                     bool lead, uint64_t tid) {
+  if (credit) credit_frees(s, blk, credit);
+  if (!lead) return false;
+  if (s->use_spares) return swap_spare(s, tree, slot, blk, tid);
+  replace_block(s, tree, slot, blk, tid);
+  return false;
+}
+
 // A block is exhausted by exactly one claim -- the one that crosses slice
 // 4095 -- and that claim's team replaces it in its pinned slot.  A team that
 // claimed from a block it read some time before (a CTA's slot_cache, or a
@@ -948,26 +961,25 @@ GAL_DEVICE_INLINE void *malloc_slices(const state *s, uint32_t tree, uint32_t co
       const bool start_valid = alloc <= SLICES_PER_BLOCK - 1;
       const bool end_valid = alloc + count <= SLICES_PER_BLOCK;
       const bool should_replace = start_valid && alloc + count > SLICES_PER_BLOCK - 1;
-      uint32_t leftover = start_valid ? (end_valid ? count - 1 : (uint32_t)(SLICES_PER_BLOCK - alloc)) : 0;
-      if (leftover) credit_frees(s, blk, leftover);  // block_correct_frees
-      uint32_t rep = __ballot_sync(live, should_replace) & team;
       const bool foreign = (uint32_t)(old >> 32) != tree;
+      const bool valid = start_valid && end_valid;
+      if (valid && !foreign) result = slice_ptr(s, blk, alloc, tree);
+      // slices this lane gives back: the rest of a run, or the part of it past
+      // the block's end (block_correct_frees), and a claimed slice of a block
+      // that serves another class now (Block::check_valid failed)
+      const uint32_t credit = (start_valid ? (end_valid ? count - 1 : (uint32_t)(SLICES_PER_BLOCK - alloc)) : 0u) +
+                              (valid && foreign ? 1u : 0u);
+      uint32_t rep = __ballot_sync(live, should_replace) & team;
       const bool exhausted = !foreign && (__ballot_sync(live, start_valid) & team) == 0;
       if (cache) {  // exhausted, replaced or foreign: the next team reads the slot again
         if ((rep || exhausted || foreign) && (int)lane == leader) atomicCAS(&cache->blk[tree], blk, NOBLK);
       }
       if (exhausted && fresh && (old & 0xFFFFFFFFull) >= SLICES_PER_BLOCK + STUCK_MARGIN)
         rep = team;  // the slot has held an exhausted block for a while: replace it here
-      if (rep && (int)lane == leader) {
-        if (s->use_spares) refill = swap_spare(s, tree, slot, blk, tid);
-        else replace_block(s, tree, slot, blk, tid);
-      }
+      const bool lead = rep && (int)lane == leader;
+      if (credit || lead) refill = claim_slow_path(s, tree, slot, blk, credit, lead, tid);
       __syncwarp(live);
       if (!NAMED && refill) refill_spare(s, tree, slot, tid);  // the team's other lanes go on
-      if (start_valid && end_valid) {
-        if ((uint32_t)(old >> 32) == tree) result = slice_ptr(s, blk, alloc, tree);
-        else credit_frees(s, blk, 1);  // Block::check_valid failed: give the slice back
-      }
     }
     if (NAMED) {
       pending = __ballot_sync(active, result == nullptr);
