@@ -203,13 +203,20 @@ int gal_bench_server(gal_handle *h, const gal_server_stream *streams, uint32_t n
   prod = grid - nsrv;
   CK(cudaMemcpy(&hs, d, sizeof(hs), cudaMemcpyDeviceToHost));
   r.cap_shift = 18;
+  // Every producer team's reservation and every server's take hits the
+  // classes' tail and taken counters.  One 32-byte sector apart, all 18 fit
+  // in five 128-byte lines, so a few L2 slices took all of that traffic and
+  // the step ran at 9.6-11.4 ms or ~7 ms depending on where the buffer
+  // landed; 4 KiB apart, 7.0-7.9 ms on seven fresh allocators (one step of
+  // 21 at 8.9 ms).
+  r.ctr_stride = 512u;
   r.deadline_ns = (uint64_t)(deadline_ms ? deadline_ms : 5000) * 1000000ull;
   CK(cudaMalloc(&r.entries, ((uint64_t)hs.num_trees << r.cap_shift) * 8));
   CK(cudaMemset(r.entries, 0, ((uint64_t)hs.num_trees << r.cap_shift) * 8));
-  CK(cudaMalloc(&counters, (uint64_t)hs.num_trees * 4 * 8 * 2));
-  CK(cudaMemset(counters, 0, (uint64_t)hs.num_trees * 4 * 8 * 2));
+  CK(cudaMalloc(&counters, (uint64_t)hs.num_trees * r.ctr_stride * 8 * 2));
+  CK(cudaMemset(counters, 0, (uint64_t)hs.num_trees * r.ctr_stride * 8 * 2));
   r.tail = counters;
-  r.taken = counters + (uint64_t)hs.num_trees * 4;
+  r.taken = counters + (uint64_t)hs.num_trees * r.ctr_stride;
   CK(cudaMalloc(&r.reply, (uint64_t)grid * SRV_BT * 8));
   CK(cudaMalloc(&flags, 64));
   CK(cudaMemset(flags, 0, 64));

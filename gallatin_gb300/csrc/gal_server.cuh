@@ -41,12 +41,13 @@ static constexpr uint32_t SERVER_BATCH = 256;
 
 struct server_rings {
   unsigned long long *entries;   // [num_trees << cap_shift]
-  unsigned long long *tail;      // positions reserved by producers, class t at t * 4 (own sector)
-  unsigned long long *taken;     // positions taken by servers, class t at t * 4
+  unsigned long long *tail;      // positions reserved by producers, class t at t * ctr_stride
+  unsigned long long *taken;     // positions taken by servers, class t at t * ctr_stride
   unsigned long long *reply;     // per reply slot: 0 pending, 1 no memory, else the pointer
   uint32_t *producers_left;      // producer CTAs not yet finished
   uint32_t *status;              // SERVER_ERR_* bits
   uint32_t cap_shift;            // ring capacity 2^cap_shift per class
+  uint32_t ctr_stride;           // words between consecutive classes' counters
   uint64_t deadline_ns;          // every wait gives up this long after the kernel began
 };
 
@@ -88,7 +89,7 @@ GAL_DEVICE_INLINE void *server_malloc(const state *s, const server_rings &r, uin
   const uint32_t team = __match_any_sync(callers, t);
   const int leader = __ffs(team) - 1;
   unsigned long long base = 0;
-  if ((int)lane_id() == leader) base = atomicAdd(r.tail + (uint64_t)t * 4, (unsigned long long)__popc(team));
+  if ((int)lane_id() == leader) base = atomicAdd(r.tail + (uint64_t)t * r.ctr_stride, (unsigned long long)__popc(team));
   base = __shfl_sync(callers, base, leader);
   const uint64_t pos = base + (uint64_t)__popc(team & lanemask_lt());
   unsigned long long *e = r.entries + ((uint64_t)t << r.cap_shift) + (pos & ((1ull << r.cap_shift) - 1));
@@ -115,10 +116,10 @@ GAL_DEVICE_INLINE void *server_malloc(const state *s, const server_rings &r, uin
 // Takes up to `most` positions of class t that producers have reserved;
 // returns how many (first position in *first).  One thread.
 GAL_DEVICE_INLINE uint32_t server_take(const server_rings &r, uint32_t t, uint32_t most, unsigned long long *first) {
-  unsigned long long *tk = r.taken + (uint64_t)t * 4;
+  unsigned long long *tk = r.taken + (uint64_t)t * r.ctr_stride;
   unsigned long long cur = ld_acquire(tk);
   for (int a = 0; a < 8; a++) {
-    const unsigned long long tl = ld_acquire(r.tail + (uint64_t)t * 4);
+    const unsigned long long tl = ld_acquire(r.tail + (uint64_t)t * r.ctr_stride);
     if (tl <= cur) return 0;
     const uint32_t m = (uint32_t)min(tl - cur, (unsigned long long)most);
     const unsigned long long seen = atomicCAS(tk, cur, cur + m);
@@ -218,7 +219,7 @@ GAL_DEVICE_INLINE void server_loop(const state *s, const server_rings &r, server
     if (lane == 0) {
       bool done = ld_rlx(r.producers_left) == 0u;
       for (uint32_t t = 0; done && t < T; t++)
-        done = ld_acquire(r.taken + (uint64_t)t * 4) >= ld_acquire(r.tail + (uint64_t)t * 4);
+        done = ld_acquire(r.taken + (uint64_t)t * r.ctr_stride) >= ld_acquire(r.tail + (uint64_t)t * r.ctr_stride);
       stop = done || global_ns() - t0 > r.deadline_ns;
       if (!stop && served == 0) __nanosleep(256);
     }
