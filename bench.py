@@ -696,7 +696,7 @@ def main():
             finally:
                 gs.close()
             server[key] = {"ops_per_s": (sr.mallocs_ok + sr.frees) / (sr.ms_total / 1e3) if sr.ms_total else None,
-                           "ms_per_step": sr.ms_total / 3, "violations": int(sr.stamp_mismatch + sr.misaligned),
+                           "ms_per_step": sr.ms_total / 3, "violations": int(sr.stamp_mismatch + sr.misaligned + sr.not_zeroed),
                            "failed": int(sr.mallocs_failed), "status": int(sr.status),
                            "error_word": int(sr.error_word),
                            "grid": int(sr.grid), "server_ctas": int(sr.server_ctas), "graph": bool(sr.graph)}

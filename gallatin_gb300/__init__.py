@@ -70,6 +70,7 @@ class ServerResult(C.Structure):
         ("stamp_mismatch", C.c_uint64),
         ("frees", C.c_uint64),
         ("misaligned", C.c_uint64),
+        ("not_zeroed", C.c_uint64),
         ("status", C.c_uint32),
         ("error_word", C.c_uint32),
         ("grid", C.c_uint32),

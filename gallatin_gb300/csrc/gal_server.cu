@@ -26,6 +26,7 @@ typedef struct gal_server_stream {
 typedef struct gal_server_result {
   double ms_total;                       /* sum over timed steps (CUDA events) */
   uint64_t mallocs_ok, mallocs_failed, stamp_mismatch, frees, misaligned;
+  uint64_t not_zeroed;                   /* zero-fill allocators: first or last word not zero */
   uint32_t status;                       /* SERVER_ERR_* bits seen           */
   uint32_t error_word;                   /* the allocator's device error word */
   uint32_t grid, server_ctas, block;
@@ -57,6 +58,7 @@ __device__ __forceinline__ uint64_t stream_size(const gal_server_stream &st, uin
 }
 
 // stats: [0] mallocs ok [1] failed [2] stamp mismatches [3] frees [4] misaligned
+// [5] not zeroed
 __device__ __forceinline__ void count(unsigned long long *c, uint32_t v) {
   if (v) atomicAdd(c, (unsigned long long)v);
 }
@@ -89,7 +91,7 @@ __global__ void __launch_bounds__(SRV_BT)
   void *kept[RING];
   uint64_t kept_id[RING], kept_size[RING];
   uint32_t nkept = 0, head = 0;
-  uint32_t ok = 0, failed = 0, bad = 0, frees = 0, misaligned = 0;
+  uint32_t ok = 0, failed = 0, bad = 0, frees = 0, misaligned = 0, not_zeroed = 0;
   for (uint64_t ch = (uint64_t)q * wpc + warp; ch < chunks; ch += (uint64_t)cp * wpc) {
     const uint64_t rq = ch * 32 + lane;
     if (rq >= st.requests) break;
@@ -104,8 +106,10 @@ __global__ void __launch_bounds__(SRV_BT)
       const uint64_t cls = 1ull << (bits < (int)s->min_shift ? s->min_shift : bits);
       const uint64_t largest = 1ull << (s->min_shift + s->num_trees - 1);
       misaligned += ((uint64_t)((char *)ptr - s->memory) % (cls < largest ? cls : largest)) != 0;
+      uint64_t *last = (uint64_t *)((char *)ptr + ((size - 8) & ~7ull));
+      if (s->zero_fill) not_zeroed += ((uint64_t *)ptr)[0] != 0ull || *last != 0ull;
       ((uint64_t *)ptr)[0] = id;
-      *(uint64_t *)((char *)ptr + ((size - 8) & ~7ull)) = id;
+      *last = id;
       kept[(head + nkept) % RING] = ptr;
       kept_id[(head + nkept) % RING] = id;
       kept_size[(head + nkept) % RING] = size;
@@ -133,6 +137,7 @@ __global__ void __launch_bounds__(SRV_BT)
   count(&stats[2], bad);
   count(&stats[3], frees);
   count(&stats[4], misaligned);
+  count(&stats[5], not_zeroed);
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
@@ -291,6 +296,7 @@ int gal_bench_server(gal_handle *h, const gal_server_stream *streams, uint32_t n
         res->stamp_mismatch += sv[2];
         res->frees += sv[3];
         res->misaligned += sv[4];
+        res->not_zeroed += sv[5];
       }
       if (status) break;  // a wait ran out: rings may hold unserved entries
     }

@@ -37,12 +37,30 @@ def test_three_producer_streams(G, direct):
         total = sum(s[0] for s in STREAMS)
         assert r.status == 0 and r.error_word == 0, r.as_dict()
         assert r.mallocs_ok == 2 * total and r.mallocs_failed == 0, r.as_dict()
-        assert r.stamp_mismatch == 0 and r.misaligned == 0, r.as_dict()
+        assert r.stamp_mismatch == 0 and r.misaligned == 0 and r.not_zeroed == 0, r.as_dict()
         assert r.frees == r.mallocs_ok
         assert (r.server_ctas > 0) != direct
         g.trim()
         assert g.error_word() == 0, g.error_info()
         assert g.export().diff(fresh, fields=TREE_FIELDS) == []
+    finally:
+        g.close()
+
+
+@pytest.mark.parametrize("direct", [False, True], ids=["server", "direct"])
+def test_zero_fill_reaches_every_served_slice(G, direct):
+    """With zero fill on, every slice a producer receives reads zero at both
+    ends before it stamps them, through the server (which fills a slice
+    before its reply) and through the direct call alike; slices come back
+    stamped by earlier requests, so a missed fill shows."""
+    g = G.Gallatin.generate_on_device(64 << 30, 42, spare_blocks=1, pinned_slots_first=0,
+                                      bytes_per_segment=64 << 20, gather_unlocked_below=16, zero_fill=1)
+    try:
+        ms, r = g.bench_server(STREAMS, server_pct=25, direct=direct, use_graph=True, warmup=1, steps=2)
+        total = sum(s[0] for s in STREAMS)
+        assert r.status == 0 and r.error_word == 0, r.as_dict()
+        assert r.mallocs_ok == 2 * total and r.mallocs_failed == 0, r.as_dict()
+        assert r.not_zeroed == 0 and r.stamp_mismatch == 0 and r.misaligned == 0, r.as_dict()
     finally:
         g.close()
 
