@@ -75,15 +75,23 @@ GAL_DEVICE_INLINE unsigned long long ring_free(uint64_t pos, uint32_t cap_shift)
   return ring_lap(pos, cap_shift) << 40;
 }
 
-// A producer lane's request for `size` bytes, answered by a server CTA of the
-// same launch.  `slot` is the lane's own reply slot (one request in flight per
-// slot).  Sizes that are not single slices take the per-thread path.  Called
-// by any subset of a warp's lanes; `t0` is the kernel's start time.
-GAL_DEVICE_INLINE void *server_malloc(const state *s, const server_rings &r, uint64_t size, uint64_t slot,
-                                      uint64_t t0) {
+// A producer lane's request for `size` bytes, sent to the server CTAs of the
+// same launch: returns true once the request is in its class's ring (its
+// answer then comes from server_wait on the same `slot`), false when it was
+// served here (*direct: sizes that are not single slices take the per-thread
+// path) or the wait for a free entry ran out (*direct = nullptr).  `slot` is
+// a reply slot of the lane's own, with one request in flight per slot; a lane
+// may post into several slots before it waits.  Called by any subset of a
+// warp's lanes; `t0` is the kernel's start time.
+GAL_DEVICE_INLINE bool server_post(const state *s, const server_rings &r, uint64_t size, uint64_t slot, uint64_t t0,
+                                   void **direct) {
   const int bits = ceil_log2(size);
   const int t = (size >> s->min_shift) == 0 ? 0 : bits - (int)s->min_shift;
-  if (t >= (int)s->num_trees) return gal::malloc(s, size);
+  *direct = nullptr;
+  if (t >= (int)s->num_trees) {
+    *direct = gal::malloc(s, size);
+    return false;
+  }
   r.reply[slot] = 0ull;
   const uint32_t callers = active_lanes();
   const uint32_t team = __match_any_sync(callers, t);
@@ -97,11 +105,17 @@ GAL_DEVICE_INLINE void *server_malloc(const state *s, const server_rings &r, uin
   for (uint32_t i = 0; ld_acquire(e) != mine; i++) {  // the previous lap's request still unserved
     if (global_ns() - t0 > r.deadline_ns) {
       atomicOr(r.status, SERVER_ERR_TIMEOUT);
-      return nullptr;
+      return false;
     }
     __nanosleep(i < 4 ? 64 : 512);
   }
   st_release(e, ring_entry(pos, r.cap_shift, slot));
+  return true;
+}
+
+// The answer to the request posted into `slot` (nullptr: no memory, or the
+// wait ran out).
+GAL_DEVICE_INLINE void *server_wait(const server_rings &r, uint64_t slot, uint64_t t0) {
   unsigned long long v;
   for (uint32_t i = 0; (v = ld_acquire(r.reply + slot)) == 0ull; i++) {
     if (global_ns() - t0 > r.deadline_ns) {
@@ -111,6 +125,13 @@ GAL_DEVICE_INLINE void *server_malloc(const state *s, const server_rings &r, uin
     __nanosleep(i < 8 ? 32 : 256);
   }
   return v == 1ull ? nullptr : (void *)v;
+}
+
+// One request, posted and waited for.
+GAL_DEVICE_INLINE void *server_malloc(const state *s, const server_rings &r, uint64_t size, uint64_t slot,
+                                      uint64_t t0) {
+  void *direct;
+  return server_post(s, r, size, slot, t0, &direct) ? server_wait(r, slot, t0) : direct;
 }
 
 // Takes up to `most` positions of class t that producers have reserved;

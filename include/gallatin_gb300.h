@@ -229,7 +229,13 @@ int gal_print_stats(gal_handle *h);
  * on invariant breaks (gallatin.cuh:87). */
 int gal_last_error(gal_handle *h, uint32_t *out_bits);
 int gal_clear_error(gal_handle *h);
-/* First recorded error: out4 = {site, value a, value b, recorded flag}. */
+/* First recorded error: out4 = {site, value a, value b, recorded flag}.
+ * Sites: 1 a block returned to a segment of no class (a: block, b: tree id);
+ * 2-5 frees (overflowing a block's count, outside the arena, into a free
+ * segment, of a segment run twice); 6 a block request whose class lock
+ * stayed taken past spin_limit (a: class, b: spins); 7 a block request whose
+ * listed segments kept refusing a block (a: class, b: last segment); 8 a
+ * segment-run request whose lock stayed taken (a: segments wanted). */
 int gal_error_info(gal_handle *h, uint64_t *out4);
 
 /* State view export/import (no reference counterpart: a snapshot of every

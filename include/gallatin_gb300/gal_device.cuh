@@ -215,6 +215,9 @@ enum : uint64_t {
   SITE_FREE_OUTSIDE = 3,
   SITE_FREE_FREE_SEGMENT = 4,
   SITE_FREE_RUN_TWICE = 5,
+  SITE_REQUEST_LOCK = 6,   // request_block: the class lock stayed taken (a: class, b: spins)
+  SITE_REQUEST_RETRY = 7,  // request_block: listed segments kept refusing a block (a: class, b: last segment)
+  SITE_RUN_LOCK = 8,       // malloc_segment_run: the run lock stayed taken (a: segments wanted)
 };
 GAL_DEVICE_INLINE void backoff(uint32_t i) { __nanosleep(i < 8 ? 32u << i : 4096u); }
 
@@ -679,7 +682,7 @@ GAL_DEVICE_COLD uint32_t request_block(const state *s, uint32_t tree, uint64_t t
         seg = (uint64_t)got;
       } else {
         if (++spins > s->spin_limit) {
-          set_error(s, GAL_DEV_ERR_TIMEOUT);
+          set_error_info(s, GAL_DEV_ERR_TIMEOUT, SITE_REQUEST_LOCK, tree, spins);
           return NOBLK;
         }
         backoff(spins);
@@ -698,7 +701,7 @@ GAL_DEVICE_COLD uint32_t request_block(const state *s, uint32_t tree, uint64_t t
     }
     if (blk != NOBLK) return blk;
     if (++spins > s->spin_limit) {
-      set_error(s, GAL_DEV_ERR_TIMEOUT);
+      set_error_info(s, GAL_DEV_ERR_TIMEOUT, SITE_REQUEST_RETRY, tree, seg);
       return NOBLK;
     }
     backoff(spins);
@@ -1015,7 +1018,7 @@ GAL_DEVICE_COLD void *malloc_segment_run(const state *s, uint32_t count) {
     uint32_t spins = 0;
     while (!try_lock(s, s->num_trees)) {
       if (++spins > s->spin_limit) {
-        set_error(s, GAL_DEV_ERR_TIMEOUT);
+        set_error_info(s, GAL_DEV_ERR_TIMEOUT, SITE_RUN_LOCK, count, spins);
         return nullptr;
       }
       backoff(spins);
