@@ -83,7 +83,7 @@ def workload_config(n, r, arena):
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=30)
+    p.add_argument("--steps", type=int, default=200)  # ~1 s timed: ~20 clock samples
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--threads-per-round", type=int, default=N_PER_ROUND)
