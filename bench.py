@@ -691,7 +691,7 @@ def main():
         for key, direct in (("server", False), ("direct", True)):
             gs = G.Gallatin.generate_on_device(64 << 30, ALLOC_SEED, **TUNED)
             try:
-                sms, sr = gs.bench_server(SERVER_STREAMS, server_pct=10, direct=direct, use_graph=True,
+                sms, sr = gs.bench_server(SERVER_STREAMS, server_pct=20, direct=direct, use_graph=True,
                                           warmup=1, steps=3)
             finally:
                 gs.close()
@@ -702,6 +702,7 @@ def main():
                            "grid": int(sr.grid), "server_ctas": int(sr.server_ctas), "graph": bool(sr.graph)}
             progress(f"server {key} done")
         server["streams"] = [list(s) for s in SERVER_STREAMS]
+        server["server_pct"] = 20
 
     # hot-word layout: L2 atomics/s on 8-byte counters, each hit by warps of
     # its own, packed 1, 2 or 4 to a 32-byte sector (304 counters: two per SM,

@@ -40,8 +40,14 @@ constexpr int MAX_STREAMS = 4;
 constexpr int SRV_BT = 256;
 constexpr int KEEP_MAX = 4;
 
+// Producer CTAs [begin[i], begin[i + 1]) of the producers serve stream i:
+// each stream's share is in proportion to its requests (at least one CTA), as
+// a producer kernel per stream would be sized for its own work.  (An equal
+// share left the largest stream's lanes with the most requests each, and they
+// alone set the step's length.)
 struct streams_param {
   gal_server_stream s[MAX_STREAMS];
+  uint32_t begin[MAX_STREAMS + 1];
   uint32_t n;
 };
 
@@ -77,10 +83,11 @@ __global__ void __launch_bounds__(SRV_BT)
     if (!direct) gal::server_loop(s, r, sm, t0);
     return;
   }
-  const uint32_t pc = blockIdx.x - server_ctas, P = gridDim.x - server_ctas;
-  const uint32_t p = pc % sp.n;
+  const uint32_t pc = blockIdx.x - server_ctas;
+  uint32_t p = 0;
+  while (p + 1 < sp.n && pc >= sp.begin[p + 1]) p++;
   const gal_server_stream st = sp.s[p];
-  const uint32_t q = pc / sp.n, cp = (P - p + sp.n - 1) / sp.n;  // this CTA among its stream's
+  const uint32_t q = pc - sp.begin[p], cp = sp.begin[p + 1] - sp.begin[p];  // this CTA among its stream's
   const uint32_t wpc = SRV_BT / 32, warp = threadIdx.x / 32, lane = threadIdx.x & 31u;
   const uint64_t slot = (uint64_t)blockIdx.x * SRV_BT + threadIdx.x;  // this lane's reply slot
   const uint64_t chunks = (st.requests + 31) / 32;
@@ -206,14 +213,32 @@ int gal_bench_server(gal_handle *h, const gal_server_stream *streams, uint32_t n
   if (!direct && nsrv < 1) nsrv = 1;
   if (nsrv >= grid) return GAL_ERR_ARGS;
   prod = grid - nsrv;
+  if (prod < nstreams) return GAL_ERR_ARGS;
+  {  // each stream one CTA, the rest in proportion to the requests (largest remainders)
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < nstreams; i++) total += streams[i].requests;
+    uint32_t cnt[MAX_STREAMS], given = 0;
+    for (uint32_t i = 0; i < nstreams; i++) {
+      cnt[i] = 1u + (uint32_t)(total ? (uint64_t)(prod - nstreams) * streams[i].requests / total : 0);
+      given += cnt[i];
+    }
+    while (given < prod) {  // fewer than nstreams left: to the most requests per CTA
+      uint32_t best = 0;
+      for (uint32_t i = 1; i < nstreams; i++)
+        if ((double)streams[i].requests / cnt[i] > (double)streams[best].requests / cnt[best]) best = i;
+      cnt[best]++;
+      given++;
+    }
+    sp.begin[0] = 0;
+    for (uint32_t i = 0; i < nstreams; i++) sp.begin[i + 1] = sp.begin[i] + cnt[i];
+  }
   CK(cudaMemcpy(&hs, d, sizeof(hs), cudaMemcpyDeviceToHost));
   r.cap_shift = 18;
   // Every producer team's reservation and every server's take hits the
   // classes' tail and taken counters.  One 32-byte sector apart, all 18 fit
-  // in five 128-byte lines, so a few L2 slices took all of that traffic and
-  // the step ran at 9.6-11.4 ms or ~7 ms depending on where the buffer
-  // landed; 4 KiB apart, 7.0-7.9 ms on seven fresh allocators (one step of
-  // 21 at 8.9 ms).
+  // in five 128-byte lines, so a few L2 slices took all of that traffic: the
+  // step ran at 9.6-11.4 ms on three allocators of four, against 7.0-7.9 ms
+  // on seven in a row with the counters 4 KiB apart.
   r.ctr_stride = 512u;
   r.deadline_ns = (uint64_t)(deadline_ms ? deadline_ms : 5000) * 1000000ull;
   CK(cudaMalloc(&r.entries, ((uint64_t)hs.num_trees << r.cap_shift) * 8));
